@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Benchmark of the plain burn path on the large polygon fill.
+
+Workload (one "step"): 100,000 seeded star polygons with 0-3 holes (outer
+ring 16-512 vertices, holes 8-64, radius lognormal median 20 px, max
+2,000 px) over a 20,000 x 20,000 raster at resolution 1, burned twice on the
+same inputs: pixel function 'sum' into float64 (NaN background) and 'count'
+into uint32 (background 0).
+
+  value : burned px/s (pixel writes per second) with inputs resident in HBM
+          and rasters left on the device, CUDA events on the engine stream
+  e2e   : the same metric through the public host API (rasterize_table) from
+          pinned host buffers, H2D of the geometry and D2H of both rasters
+          inside the timed region
+  cpu_baseline / --impl reference : the CPU restatement of the reference
+          (oracle/), timed on this host on the same workload
+
+Multi-GPU (torchrun, N > 1): every rank burns its own independent job
+(seed + rank); no data-path collective ("scaling": "weak").
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = "large_fill_100k_polygons_20000x20000_sum_f64+count_u32"
+METRIC = "burned px/s (large polygon fill: sum f64 + count u32)"
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def _workload(seed: int, scale: float):
+    from rusterize_gb300 import synth
+
+    w_sum = synth.large_fill(seed=seed, scale=scale, fn="sum")
+    return w_sum
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in self.path.read_text().splitlines():
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    mx = float(parts[1])
+                except ValueError:
+                    continue
+                for name, val in zip(names, parts[4:8]):
+                    if val.lower() == "active":
+                        reasons.add(name)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "fallback": True}
+
+
+def _oracle_step(w_sum, info, threads: int = 2) -> tuple[float, int, int]:
+    """One step of the CPU restatement: sum f64 and count u32 (independent
+    calls, run in `threads` host threads).  Returns (seconds, px, edges)."""
+    import oracle
+
+    jobs = [("sum", "float64", w_sum.values, np.nan), ("count", "uint32", None, 0)]
+    counters = [dict() for _ in jobs]
+
+    def run(i):
+        fn, dt, vals, bg = jobs[i]
+        oracle.rasterize(w_sum.table, info.nrows, info.ncols, info.xmin, info.xmax, info.ymin, info.ymax, info.xres,
+                         info.yres, values=vals, fn=fn, background=bg, dtype=dt, counters=counters[i])
+
+    t0 = time.perf_counter()
+    if threads > 1:
+        ts = [threading.Thread(target=run, args=(i,)) for i in range(len(jobs))]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+    else:
+        for i in range(len(jobs)):
+            run(i)
+    dt_s = time.perf_counter() - t0
+    return dt_s, sum(c["pixel_writes"] for c in counters), sum(c["edges"] for c in counters)
+
+
+def run_reference(args) -> None:
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    import rusterize_gb300 as rz
+
+    w = _workload(1002, args.scale)
+    info = rz.raster_info(w.table, res=w.res, extent=w.extent)
+    for _ in range(args.warmup):
+        _oracle_step(w, info)
+    times, px, edges = [], 0, 0
+    for _ in range(args.steps):
+        s, px, edges = _oracle_step(w, info)
+        times.append(s)
+    ms = 1e3 * sum(times) / len(times)
+    value = px / (ms / 1e3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "px/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "scale": args.scale},
+        "edges_per_s": edges / (ms / 1e3),
+        "cpu_baseline": {"value": value, "unit": "px/s", "cores": 2, "kind": "port",
+                         "sample": "full workload per step: the two burns (sum, count) run in 2 host threads, "
+                                   "each single-threaded like the reference's single-band process loop"},
+        "e2e": {"value": value, "unit": "px/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args) -> None:
+    import torch
+
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import rusterize_gb300 as rz
+    from rusterize_gb300 import _lib
+    from rusterize_gb300.device import DeviceTable, rasterize_device, upload
+
+    ctx = _lib.Context(local)
+    w = _workload(1002 + rank, args.scale)
+    info = rz.raster_info(w.table, res=w.res, extent=w.extent)
+    dtab = DeviceTable.upload(w.table, device=local)
+    dvals = upload(w.values, device=local)
+    out_sum = torch.empty((1, info.nrows, info.ncols), dtype=torch.float64, device=f"cuda:{local}")
+    out_cnt = torch.empty((1, info.nrows, info.ncols), dtype=torch.int32, device=f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+
+    def step(stats_acc=None):
+        st1, st2 = {}, {}
+        rasterize_device(dtab, info, fn="sum", background=np.nan, dtype="float64", values=dvals, out=out_sum,
+                         context=ctx, stats=st1)
+        rasterize_device(dtab, info, fn="count", background=0, dtype="uint32", out=out_cnt, context=ctx, stats=st2)
+        if stats_acc is not None:
+            stats_acc.append((st1, st2))
+        return st1, st2
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    acc: list = []
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step(acc)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    px_step = sum(s1["pixel_writes"] + s2["pixel_writes"] for s1, s2 in acc) / len(acc)
+    edges_step = sum(s1["edges"] + s2["edges"] for s1, s2 in acc) / len(acc)
+    launches = sum(s1["kernel_launches"] + s2["kernel_launches"] for s1, s2 in acc)
+    phase = {k: float(np.mean([s1[k] + s2[k] for s1, s2 in acc]))
+             for k in ("ms_prep", "ms_spans", "ms_bucket", "ms_fill")}
+    fill_bytes = acc[0][0]["out_bytes"] + acc[0][1]["out_bytes"]
+    span_bytes = 8 * (acc[0][0]["spans"] + acc[0][1]["spans"])
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * px_step / (ms / 1e3)
+
+    # e2e: public host API from pinned buffers (H2D + D2H inside the region)
+    e2e = None
+    if args.e2e:
+        def pinned(a, fill=True):
+            buf = torch.empty(max(1, a.nbytes), dtype=torch.uint8, pin_memory=True)
+            arr = buf.numpy()[: a.nbytes].view(a.dtype).reshape(a.shape)
+            if fill:
+                arr[...] = a
+            return arr
+
+        tb = w.table
+        ptab = rz.GeometryTable(pinned(tb.part_offsets), pinned(tb.part_kind), pinned(tb.ring_offsets),
+                                pinned(tb.vertex_offsets), pinned(tb.ring_flags), pinned(tb.xy))
+        pvals = pinned(w.values)
+        o_sum = pinned(np.empty((1, info.nrows, info.ncols), np.float64), fill=False)
+        o_cnt = pinned(np.empty((1, info.nrows, info.ncols), np.uint32), fill=False)
+
+        def host_step():
+            rz.rasterize_table(ptab, info, values=pvals, fn="sum", background=np.nan, dtype="float64", out=o_sum,
+                               context=ctx)
+            rz.rasterize_table(ptab, info, values=None, fn="count", background=0, dtype="uint32", out=o_cnt,
+                               context=ctx)
+
+        host_step()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            host_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e_ms = e0.elapsed_time(e1) / args.e2e_steps
+        h2d = sum(a.nbytes for a in (tb.part_offsets, tb.part_kind, tb.ring_offsets, tb.vertex_offsets, tb.xy))
+        h2d = 2 * h2d + w.values.nbytes
+        e2e = {"value": world * px_step / (e_ms / 1e3), "unit": "px/s", "ms_per_step": e_ms,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(o_sum.nbytes + o_cnt.nbytes)}
+
+    peaks = _measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    # dominant kernel phase: the larger of span generation and fill
+    if phase["ms_fill"] >= phase["ms_spans"]:
+        dom, dom_ms, dom_bytes = "fill (k_fill_small/k_fill_big)", phase["ms_fill"], fill_bytes + span_bytes
+    else:
+        dom = "span generation (k_poly_spans)"
+        dom_ms = phase["ms_spans"]
+        dom_bytes = 2 * 16 * w.table.n_vertices + 12 * (acc[0][0]["spans"] + acc[0][1]["spans"])
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None,
+                "peak_source": "measured" if not peaks.get("fallback") else "fallback",
+                "fill_gbs": (fill_bytes + span_bytes) / (phase["ms_fill"] / 1e3) / 1e9,
+                "phase_ms": phase}
+
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_baseline:
+        s, cpx, _ = _oracle_step(w, info, threads=1)
+        cpu = {"value": cpx / s, "unit": "px/s", "cores": 1, "kind": "port",
+               "sample": "full workload (sum f64 + count u32), one host thread, oracle/ restatement"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "px/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "scale": args.scale, "polygons": w.table.n_geoms,
+                       "vertices": w.table.n_vertices, "raster": [info.nrows, info.ncols],
+                       "l2": "inputs larger than L2 (vertex table and rasters exceed 129 MB); no flush"},
+            "edges_per_s": world * edges_step / (ms / 1e3),
+            "pixel_writes_per_step": px_step,
+            "clocks": clk.summary(),
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

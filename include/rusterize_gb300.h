@@ -1,0 +1,206 @@
+/*
+ * rusterize_gb300.h -- C ABI of the GB300 (sm_103a) burn engine.
+ *
+ * This is the drop-in boundary for rusterize's burn path.  Every entry point
+ * below replaces one interface of the reference (ttrotto/rusterize), cited
+ * by file:line inside that project.  Signatures use plain pointers, sizes and
+ * enums only, so the library can be bound from ctypes, cffi, cgo, JNI, or a
+ * Rust `extern "C"` block without any PyTorch types.
+ *
+ * Threading: an rz_context owns one CUDA stream and one device scratch
+ * arena; calls on the same context are serialised by the caller, calls on
+ * different contexts may run concurrently.  All entry points return an
+ * rz_status and, on failure, write a NUL-terminated message into err/errlen
+ * (which may be NULL/0).
+ */
+#ifndef RUSTERIZE_GB300_H
+#define RUSTERIZE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RZ_ABI_VERSION 1
+
+/* Error classes.  RZ_VALUE_ERROR and RZ_RUNTIME_ERROR carry the reference's
+ * message strings (rust/src/error.rs:3-12 RusterizeError::{ValueError,
+ * RuntimeError}); the Python layer raises the same Python exception types as
+ * python/src/rusterize.rs:148-151. */
+typedef enum {
+  RZ_OK = 0,
+  RZ_VALUE_ERROR = 1,
+  RZ_RUNTIME_ERROR = 2,
+  RZ_PARSE_ERROR = 3,  /* malformed WKT/WKB (the reference panics: parse_geometry.rs:78-87) */
+  RZ_CUDA_ERROR = 4,   /* a CUDA runtime call failed */
+  RZ_NO_DEVICE = 5,    /* no usable GPU: the engine has no CPU fallback */
+  RZ_OUT_OF_MEMORY = 6,
+  RZ_INVALID_ARGUMENT = 7
+} rz_status;
+
+/* Output element types: python/src/rusterize.rs:171-182. */
+typedef enum {
+  RZ_U8 = 0, RZ_U16 = 1, RZ_U32 = 2, RZ_U64 = 3,
+  RZ_I8 = 4, RZ_I16 = 5, RZ_I32 = 6, RZ_I64 = 7,
+  RZ_F32 = 8, RZ_F64 = 9
+} rz_dtype;
+
+/* Pixel functions: rust/src/rasterization/pixel_functions.rs:8-16. */
+typedef enum {
+  RZ_SUM = 0, RZ_FIRST = 1, RZ_LAST = 2, RZ_MIN = 3, RZ_MAX = 4, RZ_COUNT = 5, RZ_ANY = 6
+} rz_pixel_fn;
+
+/* Burn-unit kinds.  A top-level geometry is a sequence of parts:
+ *   Point / MultiPoint           -> one RZ_PART_POINT part   (burn_geometry.rs:31-44)
+ *   LineString / MultiLineString -> one RZ_PART_LINE part    (:168-210, edges pooled)
+ *   Polygon / MultiPolygon       -> one RZ_PART_POLYGON part (:76-166, rings pooled, even-odd)
+ *   GeometryCollection           -> its members' parts, in order (:64-74)
+ * Polygon rings must be closed, as geo-types' Polygon::new guarantees. */
+typedef enum { RZ_PART_POINT = 0, RZ_PART_LINE = 1, RZ_PART_POLYGON = 2 } rz_part_kind;
+
+/* Flat geometry table ("parts" CSR).  All offsets are absolute indices.
+ * ring_flags bit0 marks a polygon hole; it only matters when the extent is
+ * inferred (polygon bounding boxes use exterior rings, as geo's BoundingRect
+ * does).  ring_flags may be NULL (every ring an exterior). */
+typedef struct {
+  uint64_t n_geoms, n_parts, n_rings, n_vertices;
+  const uint64_t* part_offsets;   /* [n_geoms + 1] */
+  const uint8_t* part_kind;       /* [n_parts]     */
+  const uint64_t* ring_offsets;   /* [n_parts + 1] */
+  const uint64_t* vertex_offsets; /* [n_rings + 1] */
+  const uint8_t* ring_flags;      /* [n_rings] or NULL */
+  const double* xy;               /* [2 * n_vertices], world x,y interleaved */
+} rz_geoms;
+
+/* rust/src/geo/raster.rs:8-20 RasterInfo.  Row 0 is the ymax edge. */
+typedef struct {
+  uint64_t nrows, ncols;
+  double xmin, xmax, ymin, ymax, xres, yres;
+  int32_t epsg; /* -1: none */
+  int32_t _pad;
+} rz_raster_info;
+
+/* Per-call counters and timings (device time from CUDA events on the
+ * context's stream, host time from a steady clock). */
+typedef struct {
+  uint64_t edges;         /* polygon + line edges kept by the extract_* filters */
+  uint64_t crossings;     /* polygon scanline crossings evaluated (FP64) */
+  uint64_t spans;         /* span records after tile splitting */
+  uint64_t pixel_writes;  /* pixels passed to the pixel function */
+  uint64_t buckets;       /* (band, row, column-tile) buckets */
+  uint64_t big_buckets;   /* buckets that took the block-level ordered path */
+  uint64_t out_bytes;     /* bytes of the dense raster */
+  uint32_t reruns;        /* scratch-growth reruns in this call */
+  uint32_t kernel_launches;
+  float ms_h2d, ms_prep, ms_spans, ms_bucket, ms_fill, ms_d2h, ms_device_total;
+  float ms_host_total;
+} rz_stats;
+
+/* rz_rasterize flags */
+#define RZ_FLAG_ALL_TOUCHED   (1u << 0) /* RasterizeContext.all_touched (prelude.rs:91-106) */
+#define RZ_FLAG_INPUT_DEVICE  (1u << 1) /* geometry arrays, values, bands are device pointers */
+#define RZ_FLAG_OUTPUT_DEVICE (1u << 2) /* out is a device pointer */
+#define RZ_FLAG_SCALAR_VALUE  (1u << 3) /* values points at ONE host value (FieldSource::Scalar) */
+#define RZ_FLAG_NO_TIMING     (1u << 4) /* skip CUDA-event timing */
+
+/* raster-info builder flags (RawRasterInfo fields, python/src/geo/raster.rs:6-13) */
+#define RZ_RI_SHAPE  (1u << 0)
+#define RZ_RI_RES    (1u << 1)
+#define RZ_RI_EXTENT (1u << 2)
+#define RZ_RI_TAP    (1u << 3)
+
+typedef struct rz_context rz_context;
+typedef struct rz_geom_buffer rz_geom_buffer;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* ABI version (RZ_ABI_VERSION). */
+int rz_abi_version(void);
+
+/* Human-readable build string: arch, CUDA version. */
+const char* rz_build_info(void);
+
+/* Size in bytes of one element of `dt`, or 0 for an unknown dtype. */
+size_t rz_dtype_size(rz_dtype dt);
+
+/* Replaces PixelFunction::from_str (rust/src/rasterization/pixel_functions.rs:18-33).
+ * Unknown names -> RZ_VALUE_ERROR "Unknown pixel function". */
+rz_status rz_pixel_fn_from_str(const char* name, rz_pixel_fn* out, char* err, size_t errlen);
+
+/* ---- geometry ingestion ---------------------------------------------- */
+
+/* Replaces ParsedGeometry::extract for sequences of WKT strings
+ * (python/src/geo/parse_geometry.rs:86-88,122-133).  `texts` holds n
+ * NUL-free strings given by (ptr, len).  Polygon rings are closed like
+ * geo-types' Polygon::new.  Malformed input -> RZ_PARSE_ERROR naming the
+ * item; an empty result -> RZ_VALUE_ERROR "Could not parse geometry. Only
+ * WKT or WKB formats are supported." */
+rz_status rz_parse_wkt(const char* const* texts, const size_t* lens, size_t n,
+                       rz_geom_buffer** out, char* err, size_t errlen);
+
+/* Same for ISO/extended WKB blobs (parse_geometry.rs:77-84,109-120).
+ * Geometries that geo-types cannot hold (an empty POINT) are dropped, as
+ * try_to_geometry() does. */
+rz_status rz_parse_wkb(const uint8_t* const* blobs, const size_t* lens, size_t n,
+                       rz_geom_buffer** out, char* err, size_t errlen);
+
+/* Borrow the parsed table; valid until rz_geom_buffer_free. */
+rz_status rz_geom_buffer_view(const rz_geom_buffer* buf, rz_geoms* out);
+void rz_geom_buffer_free(rz_geom_buffer* buf);
+
+/* ---- raster grid ------------------------------------------------------ */
+
+/* Replaces RawRasterInfo::build (python/src/geo/raster.rs:17-41) and
+ * RasterInfoBuilder::{build, build_with, finalize} (rust/src/geo/raster.rs:50-156).
+ * shape = {nrows, ncols}, res = {xres, yres}, extent = {xmin, ymin, xmax, ymax};
+ * each is read only when its RZ_RI_* flag is set.  Without RZ_RI_EXTENT the
+ * extent is inferred from `g` with the half-pixel buffer.  Error strings are
+ * the reference's. */
+rz_status rz_raster_info_build(const rz_geoms* g, uint32_t flags, const uint64_t* shape,
+                               const double* res, const double* extent, int32_t epsg,
+                               rz_raster_info* out, char* err, size_t errlen);
+
+/* ---- engine ----------------------------------------------------------- */
+
+/* Create a context on CUDA device `device` (its own stream and scratch
+ * arena).  Fails with RZ_NO_DEVICE when no GPU is usable. */
+rz_status rz_context_create(int device, rz_context** out, char* err, size_t errlen);
+void rz_context_destroy(rz_context* ctx);
+
+/* Release the context's cached scratch arena (it regrows on demand). */
+rz_status rz_context_trim(rz_context* ctx);
+
+/* Burn `g` into a dense (bands, nrows, ncols) C-order raster of `out_dtype`.
+ * Replaces Rasterize::rasterize / ArrayBuilder::build for DenseArray
+ * (rust/src/rasterize.rs:54-116) with its per-geometry `process` loop
+ * (rasterize.rs:162-196) and everything below it.
+ *   values       : per-geometry burn values of out_dtype ([n_geoms]), or ONE
+ *                  value with RZ_FLAG_SCALAR_VALUE, or NULL for T::one()
+ *                  (python/src/rusterize.rs:200-212).
+ *   background   : pointer to one out_dtype value (host memory).
+ *   band_of_geom : [n_geoms] band index of each geometry (the sorted `by`
+ *                  group, rasterize.rs:198-205), or NULL for a single band.
+ *   out          : caller-owned buffer of n_bands*nrows*ncols elements
+ *                  (host unless RZ_FLAG_OUTPUT_DEVICE).
+ * Errors: "Geometry and field lengths must match" etc. are checked by the
+ * caller that owns the lengths; here inconsistent tables give
+ * RZ_INVALID_ARGUMENT. */
+rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void* values,
+                       const void* background, const uint32_t* band_of_geom, uint32_t n_bands,
+                       const rz_raster_info* info, rz_pixel_fn fn, rz_dtype out_dtype,
+                       uint32_t flags, void* out, rz_stats* stats, char* err, size_t errlen);
+
+/* The context's CUDA stream (a cudaStream_t), e.g. to record CUDA events
+ * around calls or to order other work after them. */
+void* rz_context_stream(rz_context* ctx);
+
+/* Block until all work queued on the context's stream has finished. */
+rz_status rz_context_synchronize(rz_context* ctx, char* err, size_t errlen);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RUSTERIZE_GB300_H */

@@ -1,0 +1,163 @@
+// rz_device.cuh -- device-side types and helpers shared by the engine's
+// kernels (span generation, bucketing, fill).  sm_103a only.
+#pragma once
+
+#include <cooperative_groups.h>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rzd {
+
+namespace cg = cooperative_groups;
+
+// ---- tiling --------------------------------------------------------------
+// The output is cut into buckets of (band, row, column tile).  A tile is TW
+// pixels of one row; the fill kernels own one bucket at a time and write each
+// output pixel exactly once.
+constexpr int TW_SHIFT = 10;
+constexpr int TW = 1 << TW_SHIFT;
+// span payload: x0 in bits 0-11, x1 in bits 12-23 (tile-local, x1 <= TW),
+// bit 31 = the part deduplicates its writes (PixelCache semantics).
+constexpr uint32_t X_MASK = 0xFFFu;
+constexpr uint32_t DEDUP_BIT = 1u << 31;
+
+// Polygon scanline windows: per (part, row window) a parity bitmap of
+// BITMAP_WORDS 32-bit words lives in shared memory.
+constexpr int BITMAP_WORDS = 8192;
+constexpr int WR_MAX = 64;
+constexpr int POLY_THREADS = 256;
+
+// Fill: buckets with more than SMALL_MAX spans go to the block-level path,
+// which sorts up to BIG_CAP spans at a time in shared memory.
+constexpr int SMALL_MAX = 256;
+constexpr int BIG_CAP = 4096;
+constexpr int FILL_WARPS = 8;
+
+// Longest Bresenham walk one thread performs for a single segment.
+constexpr long long LINE_MAX_STEPS = 1ll << 26;
+
+enum : unsigned {
+  ERR_NONE = 0,
+  ERR_BAD_TABLE = 1,   // offsets not monotone / out of range
+  ERR_BAD_KIND = 2,
+  ERR_BAD_BAND = 3,
+  ERR_BITMAP = 4,      // crossing outside its part's bitmap (non-finite geometry)
+  ERR_TOO_WIDE = 5,    // polygon part wider than the bitmap
+  ERR_LINE_LONG = 6,   // segment needs more than LINE_MAX_STEPS steps
+};
+
+// Device control block, reset at the start of every pass.
+struct Ctrl {
+  unsigned long long span_count;
+  unsigned long long pixel_writes;
+  unsigned long long crossings;
+  unsigned long long edges;
+  unsigned long long work;       // polygon window work counter
+  unsigned long long err_index;
+  unsigned int err;
+  unsigned int big_count;
+  unsigned long long pad[10];
+};
+
+struct Grid {
+  double xmin, ymax, xres, yres, inv_xres, inv_yres;
+  int pow2_x, pow2_y;
+  int nrows, ncols;
+  unsigned ntx;      // column tiles per row
+  unsigned n_bands;
+};
+
+struct Geo {
+  const unsigned long long* part_offsets;
+  const unsigned char* part_kind;
+  const unsigned long long* ring_offsets;
+  const unsigned long long* vertex_offsets;
+  const double2* xy;
+  const unsigned* bands;  // per geometry, or nullptr
+  unsigned long long n_geoms, n_parts, n_rings, n_vertices;
+};
+
+// Per-part plan written by the prep kernel.
+struct PartPlan {
+  int row0, row1;  // polygon rows [row0, row1)
+  int col0;        // bitmap column origin
+  int bw;          // bitmap words per row
+  int wr;          // rows per window
+  unsigned band;   // output band of the part
+};
+
+// Part-level counters, scanned (exclusive) into offsets.
+enum { PC_WINDOWS = 0, PC_LINE_V, PC_POINT_V, PC_LINE_P, PC_POINT_P, PC_N };
+
+struct SpanBuf {
+  unsigned* bucket;
+  unsigned* part;
+  unsigned* xs;
+  unsigned long long cap;
+};
+
+__device__ __forceinline__ void set_error(Ctrl* c, unsigned code, unsigned long long idx) {
+  if (atomicCAS(&c->err, 0u, code) == 0u) c->err_index = idx;
+}
+
+// world -> pixel, edges.rs:94-97 (no FMA).  A power-of-two resolution divides
+// exactly like a multiplication by its reciprocal, so that path is identical.
+__device__ __forceinline__ double to_px(const Grid& g, double wx) {
+  double d = __dsub_rn(wx, g.xmin);
+  return g.pow2_x ? __dmul_rn(d, g.inv_xres) : __ddiv_rn(d, g.xres);
+}
+__device__ __forceinline__ double to_py(const Grid& g, double wy) {
+  double d = __dsub_rn(g.ymax, wy);
+  return g.pow2_y ? __dmul_rn(d, g.inv_yres) : __ddiv_rn(d, g.yres);
+}
+
+// `(y - 0.5).ceil() as usize`, clamped to [0, nrows] (edges.rs:32-33).
+__device__ __forceinline__ int row_ceil(double py, int nrows) {
+  double c = ceil(__dsub_rn(py, 0.5));
+  if (!(c > 0.0)) return 0;
+  if (c >= (double)nrows) return nrows;
+  return (int)c;
+}
+
+// Rust f64::min / f64::max (NaN-ignoring)
+__device__ __forceinline__ double min_rs(double a, double b) {
+  return isnan(a) ? b : (isnan(b) ? a : (a < b ? a : b));
+}
+__device__ __forceinline__ double max_rs(double a, double b) {
+  return isnan(a) ? b : (isnan(b) ? a : (a > b ? a : b));
+}
+
+// Rust `f64 as isize` (saturating; NaN -> 0)
+__device__ __forceinline__ long long as_isize(double v) {
+  if (isnan(v)) return 0;
+  if (v <= -9223372036854775808.0) return (long long)0x8000000000000000ull;
+  if (v >= 9223372036854775808.0) return 0x7FFFFFFFFFFFFFFFll;
+  return (long long)v;
+}
+
+// Emit one span [xs, xe) of row `y` in `band` for `part`, cut at tile
+// boundaries.  Slots are taken with warp-aggregated atomics.
+__device__ __forceinline__ void emit_span(const SpanBuf& sb, unsigned* bucket_count, Ctrl* ctrl,
+                                          const Grid& g, unsigned band, int y, int xs, int xe,
+                                          unsigned part, unsigned flags) {
+  const unsigned long long rowid = (unsigned long long)band * (unsigned)g.nrows + (unsigned)y;
+  for (int t = xs >> TW_SHIFT; (t << TW_SHIFT) < xe; ++t) {
+    const int base = t << TW_SHIFT;
+    const unsigned a = (unsigned)(max(xs, base) - base);
+    const unsigned b = (unsigned)(min(xe, base + TW) - base);
+    const unsigned bucket = (unsigned)(rowid * g.ntx + (unsigned)t);
+    cg::coalesced_group grp = cg::coalesced_threads();
+    unsigned long long slot0 = 0;
+    if (grp.thread_rank() == 0) slot0 = atomicAdd(&ctrl->span_count, (unsigned long long)grp.size());
+    slot0 = grp.shfl(slot0, 0);
+    const unsigned long long slot = slot0 + grp.thread_rank();
+    if (slot < sb.cap) {
+      sb.bucket[slot] = bucket;
+      sb.part[slot] = part;
+      sb.xs[slot] = a | (b << 12) | flags;
+    }
+    atomicAdd(&bucket_count[bucket], 1u);
+  }
+}
+
+}  // namespace rzd

@@ -1,0 +1,494 @@
+// rz_fill.cuh -- bucket fill: every (band, row, column-tile) bucket is staged
+// in shared memory as `background`, its spans are applied in part order
+// (= the reference's per-geometry write order, rasterize.rs:162-196) with
+// the pixel function, and the tile is written to the raster once.
+//
+// Pixel functions restate rust/src/rasterization/pixel_functions.rs:56-122
+// (integer `+=` wraps, as in a release build of the crate).
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+
+#include "rz_device.cuh"
+
+namespace rzd {
+
+struct FillArgs {
+  const unsigned* offsets;  // [nbuckets + 1]
+  const uint2* spans;       // {part, xs} grouped by bucket
+  unsigned long long nbuckets;
+  const void* values;       // per-geometry values, or nullptr
+  unsigned long long scalar;  // raw bits of the single value when values == nullptr
+  const unsigned* part_geom;
+  void* out;                // (bands, nrows, ncols)
+  unsigned long long bg;    // raw bits of the background
+  uint4 bg16;               // background replicated over 16 bytes
+  int nrows, ncols;
+  unsigned ntx;
+  unsigned* big;            // buckets left to the block-level kernel
+  Ctrl* ctrl;
+  unsigned long long span_cap;
+};
+
+template <typename T> __device__ __forceinline__ bool is_nan_v(T v) { return false; }
+template <> __device__ __forceinline__ bool is_nan_v<float>(float v) { return isnan(v); }
+template <> __device__ __forceinline__ bool is_nan_v<double>(double v) { return isnan(v); }
+
+template <typename T> __device__ __forceinline__ T add_wrap(T a, T b) {
+  if constexpr (std::is_integral<T>::value) {
+    using U = typename std::make_unsigned<T>::type;
+    return (T)(U)((U)a + (U)b);
+  } else {
+    return a + b;
+  }
+}
+
+template <typename T> __device__ __forceinline__ T from_bits(unsigned long long b) {
+  T v;
+  memcpy(&v, &b, sizeof(T));
+  return v;
+}
+
+enum { F_SUM = 0, F_FIRST = 1, F_LAST = 2, F_MIN = 3, F_MAX = 4, F_COUNT = 5, F_ANY = 6 };
+
+template <typename T, int FN>
+__device__ __forceinline__ void apply_px(T& cur, T v, T bg) {
+  if constexpr (FN == F_SUM) {
+    if (cur == bg || is_nan_v(cur) || is_nan_v(v)) cur = v; else cur = add_wrap(cur, v);
+  } else if constexpr (FN == F_FIRST) {
+    if (cur == bg || is_nan_v(cur)) cur = v;
+  } else if constexpr (FN == F_LAST) {
+    cur = v;
+  } else if constexpr (FN == F_MIN) {
+    if (cur == bg || is_nan_v(cur) || cur > v) cur = v;
+  } else if constexpr (FN == F_MAX) {
+    if (cur == bg || is_nan_v(cur) || cur < v) cur = v;
+  } else if constexpr (FN == F_COUNT) {
+    if (cur == bg || is_nan_v(cur)) cur = T(1); else cur = add_wrap(cur, T(1));
+  } else {
+    cur = T(1);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T value_of(const FillArgs& a, unsigned part) {
+  if (a.values) return static_cast<const T*>(a.values)[a.part_geom[part]];
+  return from_bits<T>(a.scalar);
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_val(T v, int src) {
+  if constexpr (sizeof(T) == 8) {
+    unsigned long long b;
+    memcpy(&b, &v, 8);
+    b = __shfl_sync(0xFFFFFFFFu, b, src);
+    T r;
+    memcpy(&r, &b, 8);
+    return r;
+  } else {
+    unsigned b = 0;
+    memcpy(&b, &v, sizeof(T));
+    b = __shfl_sync(0xFFFFFFFFu, b, src);
+    T r;
+    memcpy(&r, &b, sizeof(T));
+    return r;
+  }
+}
+
+// ascending bitonic sort of one key per lane
+__device__ __forceinline__ unsigned long long warp_sort32(unsigned long long key) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(0xFFFFFFFFu, key, j);
+      const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+      const unsigned long long mn = key < o ? key : o, mx = key < o ? o : key;
+      key = (lower == up) ? mn : mx;
+    }
+  }
+  return key;
+}
+
+// ascending bitonic sort of keys[0..n) (n a power of two) by one warp
+__device__ __forceinline__ void warp_sort_smem(unsigned long long* keys, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int k = 2; k <= n; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < n; i += 32) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const unsigned long long a = keys[i], b = keys[ixj];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) { keys[i] = b; keys[ixj] = a; }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ascending bitonic sort of keys[0..n) (n a power of two) by the block
+__device__ __forceinline__ void block_sort_smem(unsigned long long* keys, int n) {
+  for (int k = 2; k <= n; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const unsigned long long a = keys[i], b = keys[ixj];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) { keys[i] = b; keys[ixj] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// copy a staged tile to the raster (16-byte stores when aligned)
+template <typename T>
+__device__ __forceinline__ void store_tile(T* dst, const T* seg, int len, int lane, int nthr) {
+  if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+    const int nv = (int)((len * sizeof(T)) >> 4);
+    const uint4* s4 = reinterpret_cast<const uint4*>(seg);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (int i = lane; i < nv; i += nthr) __stcs(d4 + i, s4[i]);
+    for (int i = (int)((nv * 16) / sizeof(T)) + lane; i < len; i += nthr) dst[i] = seg[i];
+  } else {
+    for (int i = lane; i < len; i += nthr) dst[i] = seg[i];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void store_bg(T* dst, int len, const uint4& bg16, T bg, int lane, int nthr) {
+  if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+    const int nv = (int)((len * sizeof(T)) >> 4);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (int i = lane; i < nv; i += nthr) __stcs(d4 + i, bg16);
+    for (int i = (int)((nv * 16) / sizeof(T)) + lane; i < len; i += nthr) dst[i] = bg;
+  } else {
+    for (int i = lane; i < len; i += nthr) dst[i] = bg;
+  }
+}
+
+template <typename T>
+constexpr int seg_bytes() {
+  return (int)((TW * sizeof(T) + 15) / 16 * 16);
+}
+
+template <typename T, bool DEDUP>
+constexpr int small_smem_bytes() {
+  return FILL_WARPS * (seg_bytes<T>() + SMALL_MAX * 8 + (DEDUP ? TW * 4 : 0));
+}
+
+// span apply by one warp: lane l owns the tile columns x with x % 32 == l
+template <typename T, int FN, bool DEDUP>
+__device__ __forceinline__ void warp_apply(T* seg, unsigned* mark, unsigned part, unsigned xs, T v, T bg,
+                                           int lane) {
+  const int x0 = (int)(xs & X_MASK), x1 = (int)((xs >> 12) & X_MASK);
+  int x = x0 + ((lane - x0) & 31);
+  if (DEDUP && (xs & DEDUP_BIT)) {
+    for (; x < x1; x += 32) {
+      if (mark[x] != part) { mark[x] = part; apply_px<T, FN>(seg[x], v, bg); }
+    }
+  } else {
+    for (; x < x1; x += 32) apply_px<T, FN>(seg[x], v, bg);
+  }
+}
+
+// One warp per bucket; buckets with more than SMALL_MAX spans are deferred.
+template <typename T, int FN, bool DEDUP>
+__global__ void __launch_bounds__(FILL_WARPS * 32) k_fill_small(FillArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Ctrl* ctrl = a.ctrl;
+  if (ctrl->err || ctrl->span_count > a.span_cap) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* seg = reinterpret_cast<T*>(smem + warp * seg_bytes<T>());
+  unsigned long long* keys =
+      reinterpret_cast<unsigned long long*>(smem + FILL_WARPS * seg_bytes<T>() + warp * SMALL_MAX * 8);
+  unsigned* mark = DEDUP ? reinterpret_cast<unsigned*>(smem + FILL_WARPS * (seg_bytes<T>() + SMALL_MAX * 8) +
+                                                        warp * TW * 4)
+                         : nullptr;
+  const T bg = from_bits<T>(a.bg);
+  T* out = static_cast<T*>(a.out);
+  const unsigned long long nwarps = (unsigned long long)gridDim.x * FILL_WARPS;
+  for (unsigned long long b = (unsigned long long)blockIdx.x * FILL_WARPS + warp; b < a.nbuckets; b += nwarps) {
+    const unsigned o0 = a.offsets[b];
+    const int n = (int)(a.offsets[b + 1] - o0);
+    const unsigned long long rowid = b / a.ntx;
+    const int c0 = (int)(b - rowid * a.ntx) << TW_SHIFT;
+    const int len = min(TW, a.ncols - c0);
+    T* dst = out + rowid * (unsigned long long)a.ncols + c0;
+    if (n == 0) {
+      store_bg<T>(dst, len, a.bg16, bg, lane, 32);
+      continue;
+    }
+    if (n > SMALL_MAX) {
+      if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
+      continue;
+    }
+    for (int i = lane; i < len; i += 32) seg[i] = bg;
+    if (DEDUP)
+      for (int i = lane; i < len; i += 32) mark[i] = 0xFFFFFFFFu;
+    if (n <= 32) {
+      unsigned long long key = ~0ull;
+      if (lane < n) {
+        const uint2 sp = a.spans[o0 + lane];
+        key = ((unsigned long long)sp.x << 32) | sp.y;
+      }
+      key = warp_sort32(key);
+      T v = bg;
+      if (lane < n) v = value_of<T>(a, (unsigned)(key >> 32));
+      __syncwarp();
+      for (int k = 0; k < n; ++k) {
+        const unsigned long long kk = __shfl_sync(0xFFFFFFFFu, key, k);
+        const T vk = shfl_val<T>(v, k);
+        warp_apply<T, FN, DEDUP>(seg, mark, (unsigned)(kk >> 32), (unsigned)kk, vk, bg, lane);
+      }
+    } else {
+      int np = 64;
+      while (np < n) np <<= 1;
+      for (int i = lane; i < np; i += 32) {
+        unsigned long long key = ~0ull;
+        if (i < n) {
+          const uint2 sp = a.spans[o0 + i];
+          key = ((unsigned long long)sp.x << 32) | sp.y;
+        }
+        keys[i] = key;
+      }
+      __syncwarp();
+      warp_sort_smem(keys, np);
+      for (int k0 = 0; k0 < n; k0 += 32) {
+        const int k = k0 + lane;
+        T v = bg;
+        if (k < n) v = value_of<T>(a, (unsigned)(keys[k] >> 32));
+        const int m = min(32, n - k0);
+        for (int j = 0; j < m; ++j) {
+          const unsigned long long kk = keys[k0 + j];
+          const T vk = shfl_val<T>(v, j);
+          warp_apply<T, FN, DEDUP>(seg, mark, (unsigned)(kk >> 32), (unsigned)kk, vk, bg, lane);
+        }
+      }
+    }
+    __syncwarp();
+    store_tile<T>(dst, seg, len, lane, 32);
+    __syncwarp();
+  }
+}
+
+constexpr int BIG_THREADS = 256;
+constexpr int BIG_HIST = 1024;
+
+template <typename T, bool DEDUP>
+constexpr int big_smem_bytes() {
+  return seg_bytes<T>() + BIG_CAP * 8 + BIG_CAP * (int)sizeof(T) + (DEDUP ? TW * 4 : 0) + BIG_HIST * 4;
+}
+
+// apply keys[0..m) in order: thread t owns tile columns [4t, 4t+4)
+template <typename T, int FN, bool DEDUP>
+__device__ __forceinline__ void block_apply(T* seg, unsigned* mark, const unsigned long long* keys, const T* vals,
+                                            int m, T bg) {
+  constexpr int PPT = TW / BIG_THREADS;
+  const int lo = threadIdx.x * PPT, hi = lo + PPT;
+  for (int k = 0; k < m; ++k) {
+    const unsigned long long kk = keys[k];
+    const unsigned xs = (unsigned)kk;
+    const int x0 = (int)(xs & X_MASK), x1 = (int)((xs >> 12) & X_MASK);
+    if (x1 <= lo || x0 >= hi) continue;
+    const T v = vals[k];
+    const int e = min(x1, hi);
+    if (DEDUP && (xs & DEDUP_BIT)) {
+      const unsigned part = (unsigned)(kk >> 32);
+      for (int x = max(x0, lo); x < e; ++x)
+        if (mark[x] != part) { mark[x] = part; apply_px<T, FN>(seg[x], v, bg); }
+    } else {
+      for (int x = max(x0, lo); x < e; ++x) apply_px<T, FN>(seg[x], v, bg);
+    }
+  }
+}
+
+// One block per deferred bucket.  Spans are taken in part order, at most
+// BIG_CAP at a time: a 1024-bin histogram over the part ids still pending
+// picks the largest prefix range that fits; a single part with more than
+// BIG_CAP spans is applied in chunks (its spans share one value and their
+// relative order does not change the result).
+template <typename T, int FN, bool DEDUP>
+__global__ void __launch_bounds__(BIG_THREADS) k_fill_big(FillArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Ctrl* ctrl = a.ctrl;
+  if (ctrl->err || ctrl->span_count > a.span_cap) return;
+  T* seg = reinterpret_cast<T*>(smem);
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem + seg_bytes<T>());
+  T* vals = reinterpret_cast<T*>(smem + seg_bytes<T>() + BIG_CAP * 8);
+  unsigned* mark = reinterpret_cast<unsigned*>(smem + seg_bytes<T>() + BIG_CAP * 8 + BIG_CAP * sizeof(T));
+  unsigned* hist = reinterpret_cast<unsigned*>(smem + seg_bytes<T>() + BIG_CAP * 8 + BIG_CAP * sizeof(T) +
+                                               (DEDUP ? TW * 4 : 0));
+  __shared__ unsigned s_cnt, s_min, s_max;
+  __shared__ unsigned long long s_hi;
+  __shared__ int s_single;
+  const T bg = from_bits<T>(a.bg);
+  T* out = static_cast<T*>(a.out);
+  const unsigned nbig = ctrl->big_count;
+  for (unsigned bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
+    const unsigned long long b = a.big[bi];
+    const unsigned o0 = a.offsets[b];
+    const int n = (int)(a.offsets[b + 1] - o0);
+    const unsigned long long rowid = b / a.ntx;
+    const int c0 = (int)(b - rowid * a.ntx) << TW_SHIFT;
+    const int len = min(TW, a.ncols - c0);
+    T* dst = out + rowid * (unsigned long long)a.ncols + c0;
+    for (int i = threadIdx.x; i < TW; i += BIG_THREADS) {
+      seg[i] = bg;
+      if (DEDUP) mark[i] = 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    unsigned long long lo_part = 0;  // parts < lo_part are done
+    while (true) {
+      // pending part range
+      if (threadIdx.x == 0) { s_cnt = 0; s_min = 0xFFFFFFFFu; s_max = 0; }
+      __syncthreads();
+      unsigned lmin = 0xFFFFFFFFu, lmax = 0, lcnt = 0;
+      for (int i = threadIdx.x; i < n; i += BIG_THREADS) {
+        const unsigned part = a.spans[o0 + i].x;
+        if (part >= lo_part) { lmin = min(lmin, part); lmax = max(lmax, part); ++lcnt; }
+      }
+      if (lcnt) { atomicMin(&s_min, lmin); atomicMax(&s_max, lmax); atomicAdd(&s_cnt, lcnt); }
+      __syncthreads();
+      const unsigned cnt = s_cnt;
+      if (cnt == 0) break;
+      const unsigned pmin = s_min;
+      unsigned long long pmax = s_max;
+      if (cnt <= (unsigned)BIG_CAP) {
+        if (threadIdx.x == 0) { s_hi = pmax + 1; s_single = 0; }
+      } else {
+        while (true) {
+          int shift = 0;
+          while (((pmax - pmin) >> shift) >= (unsigned long long)BIG_HIST) ++shift;
+          for (int i = threadIdx.x; i < BIG_HIST; i += BIG_THREADS) hist[i] = 0;
+          __syncthreads();
+          for (int i = threadIdx.x; i < n; i += BIG_THREADS) {
+            const unsigned part = a.spans[o0 + i].x;
+            if (part >= pmin && part <= pmax) atomicAdd(&hist[(part - pmin) >> shift], 1u);
+          }
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            unsigned cum = 0;
+            int j = -1;
+            for (int h = 0; h < BIG_HIST; ++h) {
+              if (cum + hist[h] > (unsigned)BIG_CAP) break;
+              cum += hist[h];
+              j = h;
+            }
+            s_single = 0;
+            if (j >= 0) s_hi = (unsigned long long)pmin + ((unsigned long long)(j + 1) << shift);
+            else if (shift == 0) { s_hi = (unsigned long long)pmin + 1; s_single = 1; }
+            else s_hi = 0;  // zoom into the first bin
+          }
+          __syncthreads();
+          if (s_hi != 0) break;
+          pmax = (unsigned long long)pmin + (1ull << shift) - 1;
+          __syncthreads();
+        }
+      }
+      __syncthreads();  // s_hi / s_single are written by thread 0 above
+      const unsigned long long hi = s_hi;
+      const bool single = s_single != 0;
+      __syncthreads();
+      if (!single) {
+        if (threadIdx.x == 0) s_cnt = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += BIG_THREADS) {
+          const uint2 sp = a.spans[o0 + i];
+          if (sp.x >= pmin && (unsigned long long)sp.x < hi) {
+            const unsigned slot = atomicAdd(&s_cnt, 1u);
+            keys[slot] = ((unsigned long long)sp.x << 32) | sp.y;
+          }
+        }
+        __syncthreads();
+        const int m = (int)s_cnt;
+        int np = 1;
+        while (np < m) np <<= 1;
+        for (int i = m + threadIdx.x; i < np; i += BIG_THREADS) keys[i] = ~0ull;
+        __syncthreads();
+        block_sort_smem(keys, np);
+        for (int i = threadIdx.x; i < m; i += BIG_THREADS) vals[i] = value_of<T>(a, (unsigned)(keys[i] >> 32));
+        __syncthreads();
+        block_apply<T, FN, DEDUP>(seg, mark, keys, vals, m, bg);
+        __syncthreads();
+      } else {
+        // one part with more than BIG_CAP spans: any order, in chunks
+        const T v = value_of<T>(a, pmin);
+        for (int base = 0; base < n; base += BIG_CAP) {
+          if (threadIdx.x == 0) s_cnt = 0;
+          __syncthreads();
+          for (int i = base + threadIdx.x; i < min(n, base + BIG_CAP); i += BIG_THREADS) {
+            const uint2 sp = a.spans[o0 + i];
+            if (sp.x == pmin) {
+              const unsigned slot = atomicAdd(&s_cnt, 1u);
+              keys[slot] = ((unsigned long long)sp.x << 32) | sp.y;
+              vals[slot] = v;
+            }
+          }
+          __syncthreads();
+          block_apply<T, FN, DEDUP>(seg, mark, keys, vals, (int)s_cnt, bg);
+          __syncthreads();
+        }
+      }
+      lo_part = hi;
+      __syncthreads();
+    }
+    store_tile<T>(dst, seg, len, threadIdx.x, BIG_THREADS);
+    __syncthreads();
+  }
+}
+
+// Host launcher shared by the per-dtype translation units.
+template <typename T>
+int launch_fill_t(const FillArgs& a, int fn, bool dedup, int num_sms, cudaStream_t s) {
+  int launches = 0;
+#define RZ_FILL_CASE(FNV, DD)                                                                        \
+  {                                                                                                  \
+    constexpr int ss = small_smem_bytes<T, DD>();                                                    \
+    constexpr int bs = big_smem_bytes<T, DD>();                                                      \
+    cudaFuncSetAttribute(k_fill_small<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss); \
+    cudaFuncSetAttribute(k_fill_big<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, bs);   \
+    unsigned long long want = (a.nbuckets + FILL_WARPS - 1) / FILL_WARPS;                            \
+    unsigned grid = (unsigned)(want < (unsigned long long)num_sms * 16 ? want : num_sms * 16ull);    \
+    if (grid == 0) grid = 1;                                                                         \
+    k_fill_small<T, FNV, DD><<<grid, FILL_WARPS * 32, ss, s>>>(a);                                   \
+    k_fill_big<T, FNV, DD><<<num_sms * 2, BIG_THREADS, bs, s>>>(a);                                  \
+    launches += 2;                                                                                   \
+  }
+  switch (fn) {
+    case F_SUM:
+      if (dedup) RZ_FILL_CASE(F_SUM, true) else RZ_FILL_CASE(F_SUM, false)
+      break;
+    case F_FIRST: RZ_FILL_CASE(F_FIRST, false) break;
+    case F_LAST: RZ_FILL_CASE(F_LAST, false) break;
+    case F_MIN: RZ_FILL_CASE(F_MIN, false) break;
+    case F_MAX: RZ_FILL_CASE(F_MAX, false) break;
+    case F_COUNT:
+      if (dedup) RZ_FILL_CASE(F_COUNT, true) else RZ_FILL_CASE(F_COUNT, false)
+      break;
+    default: RZ_FILL_CASE(F_ANY, false) break;
+  }
+#undef RZ_FILL_CASE
+  return launches;
+}
+
+}  // namespace rzd
+
+#define RZ_DECLARE_FILL(NAME) \
+  int NAME(const rzd::FillArgs& a, int fn, bool dedup, int num_sms, cudaStream_t s);
+RZ_DECLARE_FILL(rz_fill_u8)
+RZ_DECLARE_FILL(rz_fill_u16)
+RZ_DECLARE_FILL(rz_fill_u32)
+RZ_DECLARE_FILL(rz_fill_u64)
+RZ_DECLARE_FILL(rz_fill_i8)
+RZ_DECLARE_FILL(rz_fill_i16)
+RZ_DECLARE_FILL(rz_fill_i32)
+RZ_DECLARE_FILL(rz_fill_i64)
+RZ_DECLARE_FILL(rz_fill_f32)
+RZ_DECLARE_FILL(rz_fill_f64)

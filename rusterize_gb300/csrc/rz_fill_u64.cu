@@ -1,0 +1,6 @@
+// rz_fill_u64.cu -- fill kernels instantiated for uint64_t rasters.
+#include "rz_fill.cuh"
+
+int rz_fill_u64(const rzd::FillArgs& a, int fn, bool dedup, int num_sms, cudaStream_t s) {
+  return rzd::launch_fill_t<uint64_t>(a, fn, dedup, num_sms, s);
+}

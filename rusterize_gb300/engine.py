@@ -1,0 +1,125 @@
+"""Thin typed wrappers over the engine's C ABI: raster-grid building and the
+dense burn call.  Everything computes on the GPU; nothing here falls back to
+the CPU."""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .geometry import GeometryTable
+
+
+@dataclass
+class RasterInfo:
+    """rust/src/geo/raster.rs:8-20.  Row 0 is the ymax edge."""
+
+    nrows: int
+    ncols: int
+    xmin: float
+    xmax: float
+    ymin: float
+    ymax: float
+    xres: float
+    yres: float
+    epsg: int | None = None
+
+    def c_struct(self) -> _lib.RzRasterInfo:
+        r = _lib.RzRasterInfo()
+        r.nrows, r.ncols = self.nrows, self.ncols
+        r.xmin, r.xmax, r.ymin, r.ymax = self.xmin, self.xmax, self.ymin, self.ymax
+        r.xres, r.yres = self.xres, self.yres
+        r.epsg = -1 if self.epsg is None else int(self.epsg)
+        return r
+
+    @property
+    def shape(self) -> tuple[int, int]:
+        return (self.nrows, self.ncols)
+
+
+def raster_info(table: GeometryTable | None, shape=None, res=None, extent=None, tap: bool = False,
+                epsg: int | None = None) -> RasterInfo:
+    """RawRasterInfo::build (python/src/geo/raster.rs:17-41).  Errors are the
+    reference's RusterizeError strings, raised as ValueError/RuntimeError."""
+    lib = _lib.load()
+    flags = 0
+    c_shape = (ctypes.c_uint64 * 2)(0, 0)
+    c_res = (ctypes.c_double * 2)(0.0, 0.0)
+    c_ext = (ctypes.c_double * 4)(0.0, 0.0, 0.0, 0.0)
+    if shape is not None:
+        flags |= _lib.RI_SHAPE
+        c_shape[0], c_shape[1] = int(shape[0]), int(shape[1])
+    if res is not None:
+        flags |= _lib.RI_RES
+        c_res[0], c_res[1] = float(res[0]), float(res[1])
+    if extent is not None:
+        flags |= _lib.RI_EXTENT
+        for i in range(4):
+            c_ext[i] = float(extent[i])
+    if tap:
+        flags |= _lib.RI_TAP
+    g = table.c_view() if table is not None else None
+    out = _lib.RzRasterInfo()
+    e = _lib.errbuf()
+    st = lib.rz_raster_info_build(ctypes.byref(g) if g is not None else None, flags, c_shape, c_res, c_ext,
+                                  -1 if epsg is None else int(epsg), ctypes.byref(out), e, len(e))
+    _lib.raise_for(st, e.value)
+    return RasterInfo(out.nrows, out.ncols, out.xmin, out.xmax, out.ymin, out.ymax, out.xres, out.yres, epsg)
+
+
+def rasterize_table(table: GeometryTable, info: RasterInfo, *, values=None, fn: str = "last",
+                    background=0, dtype: str = "float64", bands: np.ndarray | None = None,
+                    n_bands: int | None = None, all_touched: bool = False,
+                    context: _lib.Context | None = None, out: np.ndarray | None = None,
+                    stats: dict | None = None) -> np.ndarray:
+    """Burn ``table`` into a dense (bands, nrows, ncols) array of ``dtype``.
+
+    values: None (burn 1), a scalar (FieldSource::Scalar) or a per-geometry
+    array of ``dtype`` (FieldSource::Array).  bands: per-geometry band index
+    (uint32) with ``n_bands`` bands, or None for one band.
+    """
+    lib = _lib.load()
+    if dtype not in _lib.DTYPES:
+        raise ValueError(f"Unsupported dtype {dtype!r}")
+    if fn not in _lib.PIXEL_FNS:
+        raise ValueError("Unknown pixel function")
+    np_dt = np.dtype(dtype)
+    ctx = context or _lib.default_context()
+    nb = 1
+    c_bands = None
+    if bands is not None:
+        bands = np.ascontiguousarray(bands, dtype=np.uint32)
+        nb = int(n_bands if n_bands is not None else (int(bands.max()) + 1 if len(bands) else 1))
+        c_bands = bands.ctypes.data
+    flags = _lib.FLAG_ALL_TOUCHED if all_touched else 0
+    vals_arr = None
+    c_vals = None
+    if values is not None:
+        if np.isscalar(values) or (isinstance(values, np.ndarray) and values.ndim == 0):
+            vals_arr = np.array([values], dtype=np_dt)
+            flags |= _lib.FLAG_SCALAR_VALUE
+        else:
+            vals_arr = np.ascontiguousarray(values, dtype=np_dt)
+            if len(vals_arr) != table.n_geoms:
+                raise ValueError("Geometry and field lengths must match")
+        c_vals = vals_arr.ctypes.data
+    bg = np.array([background], dtype=np_dt)
+    if out is None:
+        out = np.empty((nb, info.nrows, info.ncols), dtype=np_dt)
+    elif out.dtype != np_dt or out.shape != (nb, info.nrows, info.ncols) or not out.flags.c_contiguous:
+        raise ValueError("out has the wrong dtype, shape or layout")
+    g = table.c_view()
+    ri = info.c_struct()
+    st_c = _lib.RzStats()
+    e = _lib.errbuf()
+    with ctx.lock:
+        st = lib.rz_rasterize(ctx.handle, ctypes.byref(g), c_vals, bg.ctypes.data, c_bands, nb, ctypes.byref(ri),
+                              _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags, out.ctypes.data, ctypes.byref(st_c),
+                              e, len(e))
+    _lib.raise_for(st, e.value)
+    if stats is not None:
+        stats.update(st_c.as_dict())
+    return out
