@@ -6,6 +6,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "rz_bits.h"
+
 namespace rzd {
 
 namespace cg = cooperative_groups;
@@ -14,7 +16,7 @@ namespace cg = cooperative_groups;
 // The output is cut into buckets of (band, row, column tile).  A tile is TW
 // pixels of one row; the fill kernels own one bucket at a time and write each
 // output pixel exactly once.
-constexpr int TW_SHIFT = 10;
+constexpr int TW_SHIFT = 9;
 constexpr int TW = 1 << TW_SHIFT;
 // span payload: x0 in bits 0-11, x1 in bits 12-23 (tile-local, x1 <= TW),
 // bit 31 = the part deduplicates its writes (PixelCache semantics).
@@ -23,9 +25,19 @@ constexpr uint32_t DEDUP_BIT = 1u << 31;
 
 // Polygon scanline windows: per (part, row window) a parity bitmap of
 // BITMAP_WORDS 32-bit words lives in shared memory.
+// Narrow parts (bitmap row <= SMALL_BW words) take one warp per window with
+// a small bitmap; wider parts take one block per window.
 constexpr int BITMAP_WORDS = 8192;
 constexpr int WR_MAX = 64;
 constexpr int POLY_THREADS = 256;
+constexpr int POLY_QCAP = 1024;  // queued edges with crossings, per flush
+constexpr int POLY_SMEM = BITMAP_WORDS * 4 + POLY_QCAP * (3 * 8 + 2 * 4);
+constexpr int SMALL_BW = 32;
+constexpr int SMALL_BITMAP_WORDS = 1024;
+constexpr int SMALL_QCAP = 128;
+constexpr int SMALL_WARPS = 4;  // warps (independent windows) per block
+constexpr int SMALL_WARP_SMEM = SMALL_BITMAP_WORDS * 4 + SMALL_QCAP * (3 * 8 + 2 * 4) + 3 * WR_MAX * 4 + 32;
+constexpr int SMALL_SMEM = SMALL_WARPS * SMALL_WARP_SMEM;
 
 // Fill: buckets with more than SMALL_MAX spans go to the block-level path,
 // which sorts up to BIG_CAP spans at a time in shared memory.
@@ -52,11 +64,12 @@ struct Ctrl {
   unsigned long long pixel_writes;
   unsigned long long crossings;
   unsigned long long edges;
-  unsigned long long work;       // polygon window work counter
+  unsigned long long work;       // wide-part polygon window work counter
   unsigned long long err_index;
   unsigned int err;
   unsigned int big_count;
-  unsigned long long pad[10];
+  unsigned long long work_small;  // narrow-part polygon window work counter
+  unsigned long long pad[9];
 };
 
 struct Grid {
@@ -86,8 +99,9 @@ struct PartPlan {
   unsigned band;   // output band of the part
 };
 
-// Part-level counters, scanned (exclusive) into offsets.
-enum { PC_WINDOWS = 0, PC_LINE_V, PC_POINT_V, PC_LINE_P, PC_POINT_P, PC_N };
+// Part-level counters, scanned (exclusive) into offsets: polygon windows of
+// wide parts and of narrow parts, line / point vertices, line / point parts.
+enum { PC_WINDOWS = 0, PC_WIN_SMALL, PC_LINE_V, PC_POINT_V, PC_LINE_P, PC_POINT_P, PC_N };
 
 struct SpanBuf {
   unsigned* bucket;
@@ -111,13 +125,14 @@ __device__ __forceinline__ double to_py(const Grid& g, double wy) {
   return g.pow2_y ? __dmul_rn(d, g.inv_yres) : __ddiv_rn(d, g.yres);
 }
 
+using rzb::ceil_clamp;
+using rzb::f64_bits;
+using rzb::floor_clamp;
+using rzb::half_int;
+using rzb::nan_bits;
+
 // `(y - 0.5).ceil() as usize`, clamped to [0, nrows] (edges.rs:32-33).
-__device__ __forceinline__ int row_ceil(double py, int nrows) {
-  double c = ceil(__dsub_rn(py, 0.5));
-  if (!(c > 0.0)) return 0;
-  if (c >= (double)nrows) return nrows;
-  return (int)c;
-}
+__device__ __forceinline__ int row_ceil(double py, int nrows) { return ceil_clamp(__dsub_rn(py, 0.5), nrows); }
 
 // Rust f64::min / f64::max (NaN-ignoring)
 __device__ __forceinline__ double min_rs(double a, double b) {

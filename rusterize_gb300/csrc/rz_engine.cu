@@ -100,6 +100,7 @@ struct rz_context {
   int device = 0;
   int num_sms = 0;
   int poly_blocks_per_sm = 1;
+  int narrow_blocks_per_sm = 1;
   cudaStream_t stream = nullptr;
   DevBuf main, spans, out;
   cudaEvent_t ev[8] = {};
@@ -144,12 +145,25 @@ extern "C" rz_status rz_context_create(int device, rz_context** out, char* err, 
   for (int i = 0; i < 8 && e2 == cudaSuccess; ++i) e2 = cudaEventCreate(&ctx->ev[i]);
   if (e2 == cudaSuccess) e2 = cudaMallocHost((void**)&ctx->h_ctrl, sizeof(Ctrl));
   if (e2 == cudaSuccess)
-    e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->poly_blocks_per_sm, k_poly_spans, POLY_THREADS, 0);
+    e2 = cudaFuncSetAttribute(k_poly_spans, cudaFuncAttributeMaxDynamicSharedMemorySize, POLY_SMEM);
+  if (e2 == cudaSuccess)
+    e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->poly_blocks_per_sm, k_poly_spans, POLY_THREADS,
+                                                       POLY_SMEM);
+  if (e2 != cudaSuccess) {
+    rz_context_destroy(ctx);
+    return fail(err, errlen, RZ_NO_DEVICE, "CUDA initialisation failed: %s", cudaGetErrorString(e2));
+  }
+  if (e2 == cudaSuccess)
+    e2 = cudaFuncSetAttribute(k_poly_spans_narrow, cudaFuncAttributeMaxDynamicSharedMemorySize, SMALL_SMEM);
+  if (e2 == cudaSuccess)
+    e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->narrow_blocks_per_sm, k_poly_spans_narrow,
+                                                       SMALL_WARPS * 32, SMALL_SMEM);
   if (e2 != cudaSuccess) {
     rz_context_destroy(ctx);
     return fail(err, errlen, RZ_NO_DEVICE, "CUDA initialisation failed: %s", cudaGetErrorString(e2));
   }
   if (ctx->poly_blocks_per_sm < 1) ctx->poly_blocks_per_sm = 1;
+  if (ctx->narrow_blocks_per_sm < 1) ctx->narrow_blocks_per_sm = 1;
   *out = ctx;
   return RZ_OK;
 }
@@ -195,6 +209,7 @@ __global__ void k_reset_pass(Ctrl* c) {
   c->pixel_writes = 0;
   c->crossings = 0;
   c->work = 0;
+  c->work_small = 0;
   c->big_count = 0;
 }
 
@@ -392,13 +407,16 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
     launches += 1;
     if (P) {
-      k_poly_spans<<<sms * ctx->poly_blocks_per_sm, POLY_THREADS, 0, s>>>(geo, gr, plan, poff, sb, bcount, d_ctrl);
+      k_poly_spans_narrow<<<sms * ctx->narrow_blocks_per_sm, SMALL_WARPS * 32, SMALL_SMEM, s>>>(
+          geo, gr, plan, poff, sb, bcount, d_ctrl);
+      k_poly_spans<<<sms * ctx->poly_blocks_per_sm, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, plan, poff, sb, bcount,
+                                                                                  d_ctrl);
       k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept, dedup ? DEDUP_BIT : 0u, sb,
                                            bcount, d_ctrl);
       k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
                                                                dedup ? DEDUP_BIT : 0u, sb, bcount, d_ctrl);
       k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, point_parts, sb, bcount, d_ctrl);
-      launches += 4;
+      launches += 5;
     }
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[3], s));
     launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);

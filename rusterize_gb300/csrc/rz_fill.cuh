@@ -71,6 +71,41 @@ __device__ __forceinline__ void apply_px(T& cur, T v, T bg) {
   }
 }
 
+// float64 fold with the comparisons on the integer pipe: `cur == bg`, NaN
+// tests and `<`/`>` are decided on the bit patterns (IEEE: -0 == +0, NaN
+// compares false), only the accumulating add of sum/count issues FP64.
+using rzb::BgF64;
+using rzb::bg_f64;
+using rzb::eq_bg_f64;
+using rzb::gt_f64;
+
+template <int FN>
+__device__ __forceinline__ void apply_px_f64(double& cur, double v, const BgF64& bg) {
+  const unsigned long long c = f64_bits(cur);
+  if constexpr (FN == F_SUM) {
+    if (eq_bg_f64(c, bg) || nan_bits(c) || nan_bits(f64_bits(v))) cur = v; else cur = __dadd_rn(cur, v);
+  } else if constexpr (FN == F_FIRST) {
+    if (eq_bg_f64(c, bg) || nan_bits(c)) cur = v;
+  } else if constexpr (FN == F_LAST) {
+    cur = v;
+  } else if constexpr (FN == F_MIN) {
+    if (eq_bg_f64(c, bg) || nan_bits(c) || gt_f64(c, f64_bits(v))) cur = v;
+  } else if constexpr (FN == F_MAX) {
+    if (eq_bg_f64(c, bg) || nan_bits(c) || gt_f64(f64_bits(v), c)) cur = v;
+  } else if constexpr (FN == F_COUNT) {
+    if (eq_bg_f64(c, bg) || nan_bits(c)) cur = 1.0; else cur = __dadd_rn(cur, 1.0);
+  } else {
+    cur = 1.0;
+  }
+}
+
+// one pixel-function step; for float64 the background is pre-classified
+template <typename T, int FN>
+__device__ __forceinline__ void apply_one(T& cur, T v, T bg, const BgF64& bgc) {
+  if constexpr (std::is_same<T, double>::value) apply_px_f64<FN>(cur, v, bgc);
+  else apply_px<T, FN>(cur, v, bg);
+}
+
 template <typename T>
 __device__ __forceinline__ T value_of(const FillArgs& a, unsigned part) {
   if (a.values) return static_cast<const T*>(a.values)[a.part_geom[part]];
@@ -96,39 +131,7 @@ __device__ __forceinline__ T shfl_val(T v, int src) {
   }
 }
 
-// ascending bitonic sort of one key per lane
-__device__ __forceinline__ unsigned long long warp_sort32(unsigned long long key) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      const unsigned long long o = __shfl_xor_sync(0xFFFFFFFFu, key, j);
-      const bool up = (lane & k) == 0, lower = (lane & j) == 0;
-      const unsigned long long mn = key < o ? key : o, mx = key < o ? o : key;
-      key = (lower == up) ? mn : mx;
-    }
-  }
-  return key;
-}
 
-// ascending bitonic sort of keys[0..n) (n a power of two) by one warp
-__device__ __forceinline__ void warp_sort_smem(unsigned long long* keys, int n) {
-  const int lane = threadIdx.x & 31;
-  for (int k = 2; k <= n; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = lane; i < n; i += 32) {
-        const int ixj = i ^ j;
-        if (ixj > i) {
-          const unsigned long long a = keys[i], b = keys[ixj];
-          const bool up = (i & k) == 0;
-          if ((a > b) == up) { keys[i] = b; keys[ixj] = a; }
-        }
-      }
-      __syncwarp();
-    }
-  }
-}
 
 // ascending bitonic sort of keys[0..n) (n a power of two) by the block
 __device__ __forceinline__ void block_sort_smem(unsigned long long* keys, int n) {
@@ -178,43 +181,61 @@ constexpr int seg_bytes() {
   return (int)((TW * sizeof(T) + 15) / 16 * 16);
 }
 
-template <typename T, bool DEDUP>
+// ---- per-pixel fill ------------------------------------------------------
+// One warp per bucket.  Each pixel of the tile keeps the indices of up to
+// PX_K spans covering it; every lane then folds its own pixels, applying
+// those spans in part order -- exactly the reference's per-pixel write order,
+// with no per-bucket sort.  Spans longer than PX_LONG are spread over the
+// warp.  Buckets with more than SMALL_MAX spans, or with a pixel covered more
+// than PX_K times, are left to the block-level kernel.
+constexpr int PX_K = 8;
+constexpr int PX_LONG = 64;
+constexpr int PX_WARPS = 4;
+
+template <typename T>
+constexpr int px_warp_bytes() {
+  return SMALL_MAX * 8 + ((SMALL_MAX * (int)sizeof(T) + 15) / 16) * 16 + TW * 2 + TW * PX_K + SMALL_MAX;
+}
+
+template <typename T>
 constexpr int small_smem_bytes() {
-  return FILL_WARPS * (seg_bytes<T>() + SMALL_MAX * 8 + (DEDUP ? TW * 4 : 0));
+  return PX_WARPS * px_warp_bytes<T>();
 }
 
-// span apply by one warp: lane l owns the tile columns x with x % 32 == l
-template <typename T, int FN, bool DEDUP>
-__device__ __forceinline__ void warp_apply(T* seg, unsigned* mark, unsigned part, unsigned xs, T v, T bg,
-                                           int lane) {
-  const int x0 = (int)(xs & X_MASK), x1 = (int)((xs >> 12) & X_MASK);
-  int x = x0 + ((lane - x0) & 31);
-  if (DEDUP && (xs & DEDUP_BIT)) {
-    for (; x < x1; x += 32) {
-      if (mark[x] != part) { mark[x] = part; apply_px<T, FN>(seg[x], v, bg); }
-    }
-  } else {
-    for (; x < x1; x += 32) apply_px<T, FN>(seg[x], v, bg);
+// register pixel x for span i; true when the pixel list overflows
+__device__ __forceinline__ bool px_add(unsigned* depth, unsigned char* lists, int x, int i) {
+  const unsigned sh = (x & 1) * 16;
+  const unsigned d = (atomicAdd(&depth[x >> 1], 1u << sh) >> sh) & 0xFFFFu;
+  if (d < PX_K) {
+    lists[x * PX_K + d] = (unsigned char)i;
+    return false;
   }
+  return true;
 }
 
-// One warp per bucket; buckets with more than SMALL_MAX spans are deferred.
+__device__ __forceinline__ void cswap(unsigned long long& a, unsigned long long& b) {
+  const unsigned long long lo = a < b ? a : b, hi = a < b ? b : a;
+  a = lo;
+  b = hi;
+}
+
 template <typename T, int FN, bool DEDUP>
-__global__ void __launch_bounds__(FILL_WARPS * 32) k_fill_small(FillArgs a) {
+__global__ void __launch_bounds__(PX_WARPS * 32) k_fill_small(FillArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.span_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T* seg = reinterpret_cast<T*>(smem + warp * seg_bytes<T>());
-  unsigned long long* keys =
-      reinterpret_cast<unsigned long long*>(smem + FILL_WARPS * seg_bytes<T>() + warp * SMALL_MAX * 8);
-  unsigned* mark = DEDUP ? reinterpret_cast<unsigned*>(smem + FILL_WARPS * (seg_bytes<T>() + SMALL_MAX * 8) +
-                                                        warp * TW * 4)
-                         : nullptr;
+  unsigned char* base = smem + warp * px_warp_bytes<T>();
+  uint2* sp = reinterpret_cast<uint2*>(base);
+  T* vals = reinterpret_cast<T*>(base + SMALL_MAX * 8);
+  unsigned* depth = reinterpret_cast<unsigned*>(base + SMALL_MAX * 8 + ((SMALL_MAX * (int)sizeof(T) + 15) / 16) * 16);
+  unsigned char* lists = reinterpret_cast<unsigned char*>(depth + TW / 2);
+  unsigned char* longs = lists + TW * PX_K;
   const T bg = from_bits<T>(a.bg);
+  const BgF64 bgc = bg_f64(a.bg);
   T* out = static_cast<T*>(a.out);
-  const unsigned long long nwarps = (unsigned long long)gridDim.x * FILL_WARPS;
-  for (unsigned long long b = (unsigned long long)blockIdx.x * FILL_WARPS + warp; b < a.nbuckets; b += nwarps) {
+  const unsigned long long nwarps = (unsigned long long)gridDim.x * PX_WARPS;
+  for (unsigned long long b = (unsigned long long)blockIdx.x * PX_WARPS + warp; b < a.nbuckets; b += nwarps) {
     const unsigned o0 = a.offsets[b];
     const int n = (int)(a.offsets[b + 1] - o0);
     const unsigned long long rowid = b / a.ntx;
@@ -229,51 +250,78 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_fill_small(FillArgs a) {
       if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
       continue;
     }
-    for (int i = lane; i < len; i += 32) seg[i] = bg;
-    if (DEDUP)
-      for (int i = lane; i < len; i += 32) mark[i] = 0xFFFFFFFFu;
-    if (n <= 32) {
-      unsigned long long key = ~0ull;
-      if (lane < n) {
-        const uint2 sp = a.spans[o0 + lane];
-        key = ((unsigned long long)sp.x << 32) | sp.y;
+    for (int i = lane; i < n; i += 32) {
+      const uint2 s = a.spans[o0 + i];
+      sp[i] = s;
+      vals[i] = value_of<T>(a, s.x);
+    }
+    for (int i = lane; i < TW / 2; i += 32) depth[i] = 0u;
+    __syncwarp();
+    bool over = false;
+    int nlong = 0;
+    for (int i0 = 0; i0 < n; i0 += 32) {
+      const int i = i0 + lane;
+      bool lng = false;
+      if (i < n) {
+        const unsigned xs = sp[i].y;
+        const int x0 = (int)(xs & X_MASK), x1 = (int)((xs >> 12) & X_MASK);
+        if (x1 - x0 > PX_LONG) lng = true;
+        else
+          for (int x = x0; x < x1; ++x) over |= px_add(depth, lists, x, i);
       }
-      key = warp_sort32(key);
-      T v = bg;
-      if (lane < n) v = value_of<T>(a, (unsigned)(key >> 32));
-      __syncwarp();
-      for (int k = 0; k < n; ++k) {
-        const unsigned long long kk = __shfl_sync(0xFFFFFFFFu, key, k);
-        const T vk = shfl_val<T>(v, k);
-        warp_apply<T, FN, DEDUP>(seg, mark, (unsigned)(kk >> 32), (unsigned)kk, vk, bg, lane);
-      }
-    } else {
-      int np = 64;
-      while (np < n) np <<= 1;
-      for (int i = lane; i < np; i += 32) {
-        unsigned long long key = ~0ull;
-        if (i < n) {
-          const uint2 sp = a.spans[o0 + i];
-          key = ((unsigned long long)sp.x << 32) | sp.y;
-        }
-        keys[i] = key;
-      }
-      __syncwarp();
-      warp_sort_smem(keys, np);
-      for (int k0 = 0; k0 < n; k0 += 32) {
-        const int k = k0 + lane;
-        T v = bg;
-        if (k < n) v = value_of<T>(a, (unsigned)(keys[k] >> 32));
-        const int m = min(32, n - k0);
-        for (int j = 0; j < m; ++j) {
-          const unsigned long long kk = keys[k0 + j];
-          const T vk = shfl_val<T>(v, j);
-          warp_apply<T, FN, DEDUP>(seg, mark, (unsigned)(kk >> 32), (unsigned)kk, vk, bg, lane);
-        }
-      }
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, lng);
+      if (lng) longs[nlong + __popc(m & ((1u << lane) - 1u))] = (unsigned char)i;
+      nlong += __popc(m);
     }
     __syncwarp();
-    store_tile<T>(dst, seg, len, lane, 32);
+    for (int j = 0; j < nlong; ++j) {
+      const int i = longs[j];
+      const unsigned xs = sp[i].y;
+      const int x0 = (int)(xs & X_MASK), x1 = (int)((xs >> 12) & X_MASK);
+      for (int x = x0 + lane; x < x1; x += 32) over |= px_add(depth, lists, x, i);
+    }
+    if (__any_sync(0xFFFFFFFFu, over)) {
+      if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
+      __syncwarp();
+      continue;
+    }
+    __syncwarp();
+    for (int x = lane; x < len; x += 32) {
+      const unsigned d = (depth[x >> 1] >> ((x & 1) * 16)) & 0xFFFFu;
+      T cur = bg;
+      if (d) {
+        const uint2 pk = *reinterpret_cast<const uint2*>(lists + x * PX_K);
+        unsigned long long k[PX_K];
+#pragma unroll
+        for (int j = 0; j < PX_K; ++j) {
+          const unsigned idx = ((j < 4 ? pk.x : pk.y) >> (8 * (j & 3))) & 0xFFu;
+          k[j] = (unsigned)j < d ? (((unsigned long long)sp[idx].x << 32) | idx) : ~0ull;
+        }
+        // sort by (part, span index): 4-key network, or Batcher's 8-key
+        // odd-even merge network when more than 4 spans cover the pixel
+        if (d <= 4) {
+          cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[1], k[2]);
+        } else {
+          cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[4], k[5]); cswap(k[6], k[7]);
+          cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[4], k[6]); cswap(k[5], k[7]);
+          cswap(k[1], k[2]); cswap(k[5], k[6]);
+          cswap(k[0], k[4]); cswap(k[1], k[5]); cswap(k[2], k[6]); cswap(k[3], k[7]);
+          cswap(k[2], k[4]); cswap(k[3], k[5]);
+          cswap(k[1], k[2]); cswap(k[3], k[4]); cswap(k[5], k[6]);
+        }
+        unsigned prev = 0xFFFFFFFFu;
+#pragma unroll
+        for (int j = 0; j < PX_K; ++j) {
+          if ((unsigned)j < d) {
+            const unsigned idx = (unsigned)k[j] & 0xFFu, part = (unsigned)(k[j] >> 32);
+            if (DEDUP && (sp[idx].y & DEDUP_BIT) && part == prev) continue;  // PixelCache
+            prev = part;
+            apply_one<T, FN>(cur, vals[idx], bg, bgc);
+          }
+        }
+      }
+      dst[x] = cur;
+    }
     __syncwarp();
   }
 }
@@ -289,7 +337,7 @@ constexpr int big_smem_bytes() {
 // apply keys[0..m) in order: thread t owns tile columns [4t, 4t+4)
 template <typename T, int FN, bool DEDUP>
 __device__ __forceinline__ void block_apply(T* seg, unsigned* mark, const unsigned long long* keys, const T* vals,
-                                            int m, T bg) {
+                                            int m, T bg, const BgF64& bgc) {
   constexpr int PPT = TW / BIG_THREADS;
   const int lo = threadIdx.x * PPT, hi = lo + PPT;
   for (int k = 0; k < m; ++k) {
@@ -302,9 +350,9 @@ __device__ __forceinline__ void block_apply(T* seg, unsigned* mark, const unsign
     if (DEDUP && (xs & DEDUP_BIT)) {
       const unsigned part = (unsigned)(kk >> 32);
       for (int x = max(x0, lo); x < e; ++x)
-        if (mark[x] != part) { mark[x] = part; apply_px<T, FN>(seg[x], v, bg); }
+        if (mark[x] != part) { mark[x] = part; apply_one<T, FN>(seg[x], v, bg, bgc); }
     } else {
-      for (int x = max(x0, lo); x < e; ++x) apply_px<T, FN>(seg[x], v, bg);
+      for (int x = max(x0, lo); x < e; ++x) apply_one<T, FN>(seg[x], v, bg, bgc);
     }
   }
 }
@@ -329,6 +377,7 @@ __global__ void __launch_bounds__(BIG_THREADS) k_fill_big(FillArgs a) {
   __shared__ unsigned long long s_hi;
   __shared__ int s_single;
   const T bg = from_bits<T>(a.bg);
+  const BgF64 bgc = bg_f64(a.bg);
   T* out = static_cast<T*>(a.out);
   const unsigned nbig = ctrl->big_count;
   for (unsigned bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
@@ -415,7 +464,7 @@ __global__ void __launch_bounds__(BIG_THREADS) k_fill_big(FillArgs a) {
         block_sort_smem(keys, np);
         for (int i = threadIdx.x; i < m; i += BIG_THREADS) vals[i] = value_of<T>(a, (unsigned)(keys[i] >> 32));
         __syncthreads();
-        block_apply<T, FN, DEDUP>(seg, mark, keys, vals, m, bg);
+        block_apply<T, FN, DEDUP>(seg, mark, keys, vals, m, bg, bgc);
         __syncthreads();
       } else {
         // one part with more than BIG_CAP spans: any order, in chunks
@@ -432,7 +481,7 @@ __global__ void __launch_bounds__(BIG_THREADS) k_fill_big(FillArgs a) {
             }
           }
           __syncthreads();
-          block_apply<T, FN, DEDUP>(seg, mark, keys, vals, (int)s_cnt, bg);
+          block_apply<T, FN, DEDUP>(seg, mark, keys, vals, (int)s_cnt, bg, bgc);
           __syncthreads();
         }
       }
@@ -450,14 +499,14 @@ int launch_fill_t(const FillArgs& a, int fn, bool dedup, int num_sms, cudaStream
   int launches = 0;
 #define RZ_FILL_CASE(FNV, DD)                                                                        \
   {                                                                                                  \
-    constexpr int ss = small_smem_bytes<T, DD>();                                                    \
+    constexpr int ss = small_smem_bytes<T>();                                                        \
     constexpr int bs = big_smem_bytes<T, DD>();                                                      \
     cudaFuncSetAttribute(k_fill_small<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss); \
     cudaFuncSetAttribute(k_fill_big<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, bs);   \
-    unsigned long long want = (a.nbuckets + FILL_WARPS - 1) / FILL_WARPS;                            \
-    unsigned grid = (unsigned)(want < (unsigned long long)num_sms * 16 ? want : num_sms * 16ull);    \
+    unsigned long long want = (a.nbuckets + PX_WARPS - 1) / PX_WARPS;                                \
+    unsigned grid = (unsigned)(want < (unsigned long long)num_sms * 32 ? want : num_sms * 32ull);    \
     if (grid == 0) grid = 1;                                                                         \
-    k_fill_small<T, FNV, DD><<<grid, FILL_WARPS * 32, ss, s>>>(a);                                   \
+    k_fill_small<T, FNV, DD><<<grid, PX_WARPS * 32, ss, s>>>(a);                                     \
     k_fill_big<T, FNV, DD><<<num_sms * 2, BIG_THREADS, bs, s>>>(a);                                  \
     launches += 2;                                                                                   \
   }

@@ -10,6 +10,7 @@
 #pragma once
 
 #include "rz_device.cuh"
+#include "rz_poly.cuh"
 
 namespace rzd {
 
@@ -75,7 +76,7 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
     const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
     const unsigned long long vs = geo.vertex_offsets[rb], ve = geo.vertex_offsets[re];
     const unsigned band = geo.bands ? geo.bands[part_geom[p]] : 0u;
-    unsigned long long c[PC_N] = {0, 0, 0, 0, 0};
+    unsigned long long c[PC_N] = {0, 0, 0, 0, 0, 0};
     PartPlan pl = {0, 0, 0, 0, 0, band};
     if (kind != 0) {
       // segments = vertices - non-empty rings
@@ -92,29 +93,46 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
       c[PC_POINT_V] = ve - vs;
       c[PC_POINT_P] = 1;
     } else {
-      double ylo = INFINITY, yhi = -INFINITY, xlo = INFINITY, xhi = -INFINITY;
+      // min / max of the world coordinates on the integer pipe: monotone
+      // keys of the bit patterns, NaN excluded (edges with NaN never burn)
+      long long ylo = 0x7FFFFFFFFFFFFFFFll, yhi = (long long)0x8000000000000000ull;
+      long long xlo = 0x7FFFFFFFFFFFFFFFll, xhi = (long long)0x8000000000000000ull;
       int nan_x = 0;
       for (unsigned long long v = vs + lane; v < ve; v += 32) {
-        double2 w = geo.xy[v];
-        if (!isnan(w.y)) { ylo = fmin(ylo, w.y); yhi = fmax(yhi, w.y); }
-        if (!isnan(w.x)) { xlo = fmin(xlo, w.x); xhi = fmax(xhi, w.x); }
-        else nan_x = 1;
+        const double2 w = geo.xy[v];
+        const unsigned long long by = f64_bits(w.y), bx = f64_bits(w.x);
+        if (!nan_bits(by)) {
+          const long long k = (long long)(by ^ ((unsigned long long)((long long)by >> 63) >> 1));
+          ylo = min(ylo, k);
+          yhi = max(yhi, k);
+        }
+        if (!nan_bits(bx)) {
+          const long long k = (long long)(bx ^ ((unsigned long long)((long long)bx >> 63) >> 1));
+          xlo = min(xlo, k);
+          xhi = max(xhi, k);
+        } else {
+          nan_x = 1;
+        }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        ylo = fmin(ylo, __shfl_xor_sync(0xFFFFFFFFu, ylo, o));
-        yhi = fmax(yhi, __shfl_xor_sync(0xFFFFFFFFu, yhi, o));
-        xlo = fmin(xlo, __shfl_xor_sync(0xFFFFFFFFu, xlo, o));
-        xhi = fmax(xhi, __shfl_xor_sync(0xFFFFFFFFu, xhi, o));
+        ylo = min(ylo, (long long)__shfl_xor_sync(0xFFFFFFFFu, (unsigned long long)ylo, o));
+        yhi = max(yhi, (long long)__shfl_xor_sync(0xFFFFFFFFu, (unsigned long long)yhi, o));
+        xlo = min(xlo, (long long)__shfl_xor_sync(0xFFFFFFFFu, (unsigned long long)xlo, o));
+        xhi = max(xhi, (long long)__shfl_xor_sync(0xFFFFFFFFu, (unsigned long long)xhi, o));
       }
       nan_x = __any_sync(0xFFFFFFFFu, nan_x);
+      auto unkey = [](long long k) {
+        const unsigned long long b = (unsigned long long)k ^ ((unsigned long long)(k >> 63) >> 1);
+        return __longlong_as_double((long long)b);
+      };
       if (ylo <= yhi) {
         // pixel y decreases with world y
-        const int row0 = row_ceil(to_py(g, yhi), g.nrows);
-        const int row1 = row_ceil(to_py(g, ylo), g.nrows);
+        const int row0 = row_ceil(to_py(g, unkey(yhi)), g.nrows);
+        const int row1 = row_ceil(to_py(g, unkey(ylo)), g.nrows);
         if (row1 > row0) {
           double c_lo = 0.0, c_hi = (double)g.ncols;
           if (xlo <= xhi && !nan_x) {
-            const double pxl = to_px(g, xlo), pxh = to_px(g, xhi);
+            const double pxl = to_px(g, unkey(xlo)), pxh = to_px(g, unkey(xhi));
             // crossings are interpolations between edge end points; allow a
             // rounding margin that grows with the coordinate magnitude
             const double mag = fmax(fabs(pxl), fabs(pxh));
@@ -125,7 +143,8 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
           const int col0 = c_lo <= 0.0 ? 0 : (c_lo >= g.ncols ? g.ncols : (int)c_lo);
           const int colmax = c_hi <= 0.0 ? 0 : (c_hi >= g.ncols ? g.ncols : (int)c_hi);
           const int bw = (colmax - col0 + 1 + 31) >> 5;
-          int wr = BITMAP_WORDS / bw;
+          const bool narrow = bw <= SMALL_BW;
+          int wr = (narrow ? SMALL_BITMAP_WORDS : BITMAP_WORDS) / bw;
           if (wr > WR_MAX) wr = WR_MAX;
           if (wr < 1) {
             if (lane == 0) set_error(ctrl, ERR_TOO_WIDE, p);
@@ -135,7 +154,7 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
             pl.col0 = col0;
             pl.bw = bw;
             pl.wr = wr;
-            c[PC_WINDOWS] = (unsigned long long)((row1 - row0 + wr - 1) / wr);
+            c[narrow ? PC_WIN_SMALL : PC_WINDOWS] = (unsigned long long)((row1 - row0 + wr - 1) / wr);
           }
         }
       }
@@ -160,219 +179,6 @@ __global__ void k_part_lists(Geo geo, const unsigned long long* off /*[P+1][PC_N
     const unsigned kind = geo.part_kind[p];
     if (kind == 1) line_parts[off[p * PC_N + PC_LINE_P]] = (unsigned)p;
     else if (kind == 0) point_parts[off[p * PC_N + PC_POINT_P]] = (unsigned)p;
-  }
-}
-
-// -------------------------------------------------------------- polygons ----
-// One CTA per (part, row window).  Every edge crossing of a scanline centre
-// is evaluated in FP64 exactly as PolyEdge::intersect_at (edges.rs:50-55) and
-// rounded to its pixel boundary r = clamp(floor(x + 0.5), 0, ncols)
-// (burners.rs:310-311).  Because that rounding is monotone, pairing the
-// x-sorted crossings (burners.rs:302-316) covers exactly the pixels whose
-// count of boundaries r <= x is odd, so each crossing toggles bit r of a
-// per-row parity bitmap and spans are read back as consecutive set bits.
-// chunks_exact(2) drops the largest crossing of an odd row: such rows are
-// fixed up by toggling their maximum r once more.  Positive-NaN crossings
-// sort after every number (total_cmp) and pair into empty spans, so they
-// are skipped; negative NaNs round to 0 and sort first.
-template <int MODE>  // 0: toggle crossings, 1: max crossing of odd rows
-__device__ __forceinline__ void poly_edges(const Geo& geo, const Grid& g, unsigned long long rb,
-                                           unsigned long long re, int r0, int r1, int col0, int bw,
-                                           unsigned* bm, const int* rowslot, int* oddmax, Ctrl* ctrl,
-                                           unsigned long long p, unsigned long long& ncross) {
-  const int lane = threadIdx.x & 31;
-  const unsigned long long vs = geo.vertex_offsets[rb], ve = geo.vertex_offsets[re];
-  unsigned long long ring = rb;
-  const int nbits = bw * 32;
-  for (unsigned long long base = vs; base < ve; base += POLY_THREADS) {
-    const unsigned long long v = base + threadIdx.x;
-    const bool has = v < ve;
-    double2 w0 = make_double2(0.0, 0.0);
-    double py0 = 0.0;
-    int ys0 = 0;
-    if (has) {
-      w0 = geo.xy[v];
-      py0 = to_py(g, w0.y);
-      ys0 = row_ceil(py0, g.nrows);
-    }
-    // vertex v+1 from the next lane (lane 31 loads it)
-    double py1 = __shfl_down_sync(0xFFFFFFFFu, py0, 1);
-    int ys1 = __shfl_down_sync(0xFFFFFFFFu, ys0, 1);
-    if (!has) continue;
-    // ring containing v
-    if (geo.vertex_offsets[ring + 1] <= v) {
-      int steps = 0;
-      while (steps < 4 && geo.vertex_offsets[ring + 1] <= v) { ++ring; ++steps; }
-      if (geo.vertex_offsets[ring + 1] <= v) {
-        unsigned long long lo = ring, hi = re;  // vo[lo] <= v < vo[hi]
-        while (hi - lo > 1) {
-          unsigned long long mid = (lo + hi) >> 1;
-          if (geo.vertex_offsets[mid] <= v) lo = mid; else hi = mid;
-        }
-        ring = lo;
-      }
-    }
-    if (v + 1 >= geo.vertex_offsets[ring + 1]) continue;  // last vertex of its ring
-    double2 w1;
-    if (lane == 31 || v + 1 >= base + POLY_THREADS) {
-      w1 = geo.xy[v + 1];
-      py1 = to_py(g, w1.y);
-      ys1 = row_ceil(py1, g.nrows);
-    }
-    if (ys0 == ys1) continue;  // no scanline centre in [y_top, y_bot)
-    // extract_ring's horizontal filter (edges.rs:100); the raster-row filter
-    // (:105) only removes edges without rows in [0, nrows), already empty here
-    if (!(fabs(__dsub_rn(py0, py1)) >= 2.220446049250313e-16)) continue;
-    const bool top0 = ys0 < ys1;  // y0 < y1 (ceil is monotone, values differ)
-    const int ystart = top0 ? ys0 : ys1, yend = top0 ? ys1 : ys0;
-    const int a = max(ystart, r0), b = min(yend, r1);
-    if (a >= b) continue;
-    if (lane != 31 && v + 1 < base + POLY_THREADS) w1 = geo.xy[v + 1];
-    const double px0 = to_px(g, w0.x), px1 = to_px(g, w1.x);
-    const double xt = top0 ? px0 : px1, yt = top0 ? py0 : py1;
-    const double xb = top0 ? px1 : px0, yb = top0 ? py1 : py0;
-    const double dxdy = __ddiv_rn(__dsub_rn(xb, xt), __dsub_rn(yb, yt));  // edges.rs:36
-    for (int y = a; y < b; ++y) {
-      if (MODE == 1 && rowslot[y - r0] < 0) continue;
-      const double cy = __dadd_rn((double)y, 0.5);
-      const double x = __dadd_rn(xt, __dmul_rn(__dsub_rn(cy, yt), dxdy));
-      int r;
-      if (isnan(x)) {
-        if (!signbit(x)) continue;
-        r = 0;
-      } else {
-        const double f = floor(__dadd_rn(x, 0.5));
-        r = f <= 0.0 ? 0 : (f >= (double)g.ncols ? g.ncols : (int)f);
-      }
-      const int loc = r - col0;
-      if (loc < 0 || loc >= nbits) {
-        set_error(ctrl, ERR_BITMAP, p);
-        continue;
-      }
-      if (MODE == 0) {
-        atomicXor(&bm[(y - r0) * bw + (loc >> 5)], 1u << (loc & 31));
-        ++ncross;
-      } else {
-        atomicMax(&oddmax[rowslot[y - r0]], loc);
-      }
-    }
-  }
-}
-
-__global__ void __launch_bounds__(POLY_THREADS) k_poly_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
-                                                              const unsigned long long* __restrict__ poff,
-                                                              SpanBuf sb, unsigned* bucket_count, Ctrl* ctrl) {
-  __shared__ unsigned bm[BITMAP_WORDS];
-  __shared__ int rowslot[WR_MAX];
-  __shared__ int oddmax[WR_MAX];
-  __shared__ int oddrow[WR_MAX];
-  __shared__ int s_nodd;
-  __shared__ unsigned long long s_part, s_w;
-  if (ctrl->err) return;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const unsigned long long total = poff[geo.n_parts * PC_N + PC_WINDOWS];
-  unsigned long long ncross = 0, npix = 0;
-  while (true) {
-    if (threadIdx.x == 0) {
-      const unsigned long long w = atomicAdd(&ctrl->work, 1ull);
-      s_w = w;
-      if (w < total) {
-        unsigned long long lo = 0, hi = geo.n_parts;  // off[lo] <= w < off[hi]
-        while (hi - lo > 1) {
-          const unsigned long long mid = (lo + hi) >> 1;
-          if (poff[mid * PC_N + PC_WINDOWS] <= w) lo = mid; else hi = mid;
-        }
-        s_part = lo;
-      }
-      s_nodd = 0;
-    }
-    __syncthreads();
-    const unsigned long long w = s_w;
-    if (w >= total) break;
-    const unsigned long long p = s_part;
-    const PartPlan pl = plan[p];
-    const int k = (int)(w - poff[p * PC_N + PC_WINDOWS]);
-    const int r0 = pl.row0 + k * pl.wr;
-    const int r1 = min(r0 + pl.wr, pl.row1);
-    const int nr = r1 - r0, bw = pl.bw;
-    for (int i = threadIdx.x; i < nr * bw; i += POLY_THREADS) bm[i] = 0u;
-    if (threadIdx.x < WR_MAX) rowslot[threadIdx.x] = -1;
-    __syncthreads();
-    const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
-    poly_edges<0>(geo, g, rb, re, r0, r1, pl.col0, bw, bm, rowslot, oddmax, ctrl, p, ncross);
-    __syncthreads();
-    // rows with an odd number of crossings
-    for (int i = warp; i < nr; i += POLY_THREADS / 32) {
-      unsigned par = 0;
-      for (int wd = lane; wd < bw; wd += 32) par ^= (unsigned)__popc(bm[i * bw + wd]) & 1u;
-      par = __reduce_xor_sync(0xFFFFFFFFu, par);
-      if (lane == 0 && par) {
-        const int slot = atomicAdd(&s_nodd, 1);
-        rowslot[i] = slot;
-        oddrow[slot] = i;
-        oddmax[slot] = -1;
-      }
-    }
-    __syncthreads();
-    if (s_nodd > 0) {
-      unsigned long long dummy = 0;
-      poly_edges<1>(geo, g, rb, re, r0, r1, pl.col0, bw, bm, rowslot, oddmax, ctrl, p, dummy);
-      __syncthreads();
-      if (threadIdx.x < s_nodd) {
-        const int i = oddrow[threadIdx.x], loc = oddmax[threadIdx.x];
-        if (loc >= 0) bm[i * bw + (loc >> 5)] ^= 1u << (loc & 31);
-      }
-      __syncthreads();
-    }
-    // spans = pairs of consecutive set bits, one warp per row
-    for (int i = warp; i < nr; i += POLY_THREADS / 32) {
-      const int y = r0 + i;
-      unsigned carry_cnt = 0;
-      int carry_last = -1;
-      for (int wb = 0; wb < bw; wb += 32) {
-        const int wd = wb + lane;
-        unsigned bits = wd < bw ? bm[i * bw + wd] : 0u;
-        const int cnt = __popc(bits);
-        int incl = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-          const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-          if (lane >= o) incl += t;
-        }
-        const int mylast = bits ? wd * 32 + 31 - __clz(bits) : -1;
-        int mx = mylast;
-        for (int o = 1; o < 32; o <<= 1) {
-          const int t = __shfl_up_sync(0xFFFFFFFFu, mx, o);
-          if (lane >= o) mx = max(mx, t);
-        }
-        int prev = __shfl_up_sync(0xFFFFFFFFu, mx, 1);
-        if (lane == 0) prev = -1;
-        prev = max(prev, carry_last);
-        unsigned gidx = carry_cnt + (unsigned)(incl - cnt);
-        while (bits) {
-          const int b = __ffs(bits) - 1;
-          bits &= bits - 1;
-          const int pos = wd * 32 + b;
-          if (gidx & 1u) {
-            const int xs = pl.col0 + prev, xe = pl.col0 + pos;
-            npix += (unsigned long long)(xe - xs);
-            emit_span(sb, bucket_count, ctrl, g, pl.band, y, xs, xe, (unsigned)p, 0u);
-          }
-          prev = pos;
-          ++gidx;
-        }
-        carry_cnt += (unsigned)__shfl_sync(0xFFFFFFFFu, incl, 31);
-        carry_last = max(carry_last, __shfl_sync(0xFFFFFFFFu, mx, 31));
-      }
-    }
-    __syncthreads();
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    ncross += __shfl_xor_sync(0xFFFFFFFFu, ncross, o);
-    npix += __shfl_xor_sync(0xFFFFFFFFu, npix, o);
-  }
-  if (lane == 0) {
-    if (ncross) atomicAdd(&ctrl->crossings, ncross);
-    if (npix) atomicAdd(&ctrl->pixel_writes, npix);
   }
 }
 

@@ -216,16 +216,23 @@ def test_degenerate_and_nonfinite():
 
 
 def test_span_buffer_growth_rerun():
-    # > 1M spans from a handful of vertices forces the overflow-and-rerun path
+    # steep lines give one span per pixel: > 1M spans from a few hundred
+    # vertices overflow the first span buffer and force the rerun path
     rng = np.random.default_rng(4)
     b = G.TableBuilder()
-    for i in range(300):
-        y0, y1 = rng.uniform(0, 4000, 2)
-        G.add_linestring(b, [(0.5, y0), (3999.5, y1)] if i % 2 else [(y0, 0.5), (y1, 3999.5)])
+    for _ in range(400):
+        x0, x1 = rng.uniform(0, 4000, 2)
+        G.add_linestring(b, [(x0, 0.5), (x0 + (x1 - x0) * 0.25, 3999.5)])
     t = b.build()
     grid = dict(nrows=4000, ncols=4000, xmin=0.0, xmax=4000.0, ymin=0.0, ymax=4000.0, xres=1.0, yres=1.0)
-    stats = check(t, grid, fn="count", values=None, background=0, dtype="uint8")
-    assert stats["spans"] > 1_000_000
+    ctx = rz.Context(0)  # fresh scratch arena
+    stats = {}
+    got = rz.rasterize_table(t, rz.RasterInfo(**grid), fn="count", background=0, dtype="uint8", context=ctx,
+                             stats=stats)
+    ref = oracle_burn(t, grid, fn="count", background=0, dtype="uint8")
+    assert same_bits(got, ref), diff_report(got, ref)
+    assert stats["spans"] > 1_000_000 and stats["reruns"] >= 1
+    ctx.close()
 
 
 def test_repeat_calls_reuse_scratch():
