@@ -71,6 +71,53 @@ RZ_HD int ceil_clamp(double t, int hi) {
   return c > hi ? hi : (int)c;
 }
 
+// clamp(floor(fl(x + 0.5)), 0, hi) for non-NaN x, without the FP64 add:
+// the exact sum is formed on the mantissa and rounded to nearest-even the
+// way the add rounds it (only a carry into the next binade can round).
+RZ_HD int floor_half_up(double x, int hi) {
+  const uint64_t b = f64_bits(x);
+  if (b >> 63) return 0;                     // x <= -0: x + 0.5 <= 0.5
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  if (e >= 31) return hi;                    // x >= 2^31 (and +inf)
+  if (e <= -3) return 0;                     // x < 0.25
+  if (e == -2) return b == 0x3FDFFFFFFFFFFFFFull ? (hi < 1 ? hi : 1) : 0;  // 0.5 - 2^-54 ties up to 1.0
+  const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
+  const int s = 52 - e;                      // 22..53
+  const uint64_t S = m + (1ull << (s - 1));  // (x + 0.5) * 2^s, exact
+  uint64_t f;
+  if (S < (1ull << 53)) {
+    f = S >> s;
+  } else {                                   // next binade: round S/2 to even
+    uint64_t h = S >> 1;
+    if ((S & 1) && (h & 1)) h += 1;
+    f = h >> (s - 1);
+  }
+  return f > (uint64_t)hi ? hi : (int)f;
+}
+
+// clamp(ceil(fl(y - 0.5)), 0, hi), NaN -> 0, without the FP64 subtract:
+// for y >= 0.5 the difference is exact (Sterbenz / same-exponent cases).
+RZ_HD int ceil_half_down(double y, int hi) {
+  const uint64_t b = f64_bits(y);
+  if (b >> 63) return 0;
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  if (e == 1024) return (b & 0x000FFFFFFFFFFFFFull) ? 0 : hi;
+  if (e >= 31) return hi;
+  if (e < -1) return 0;                      // y < 0.5
+  if (e == -1) return b == 0x3FE0000000000000ull ? 0 : (hi < 1 ? hi : 1);  // y in [0.5, 1)
+  const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
+  const int s = 52 - e;                      // 22..52
+  const uint64_t D = m - (1ull << (s - 1));  // (y - 0.5) * 2^s, exact
+  const uint64_t c = (D + (1ull << s) - 1) >> s;
+  return c > (uint64_t)hi ? hi : (int)c;
+}
+
+// |v| >= 1 (infinities included, NaN excluded)
+RZ_HD bool abs_ge_one(double v) {
+  const uint64_t b = f64_bits(v);
+  return ((b >> 52) & 0x7FF) >= 1023 && !nan_bits(b);
+}
+
 // IEEE comparisons of f64 values given as bit patterns
 struct BgF64 {
   uint64_t bits;

@@ -74,7 +74,8 @@ struct Ctrl {
 
 struct Grid {
   double xmin, ymax, xres, yres, inv_xres, inv_yres;
-  int pow2_x, pow2_y;
+  int pow2_x, pow2_y;  // resolution a power of two: multiply by the exact reciprocal
+  int unit_x, unit_y;  // resolution 1: the division is the identity
   int nrows, ncols;
   unsigned ntx;      // column tiles per row
   unsigned n_bands;
@@ -118,21 +119,26 @@ __device__ __forceinline__ void set_error(Ctrl* c, unsigned code, unsigned long 
 // exactly like a multiplication by its reciprocal, so that path is identical.
 __device__ __forceinline__ double to_px(const Grid& g, double wx) {
   double d = __dsub_rn(wx, g.xmin);
+  if (g.unit_x) return d;
   return g.pow2_x ? __dmul_rn(d, g.inv_xres) : __ddiv_rn(d, g.xres);
 }
 __device__ __forceinline__ double to_py(const Grid& g, double wy) {
   double d = __dsub_rn(g.ymax, wy);
+  if (g.unit_y) return d;
   return g.pow2_y ? __dmul_rn(d, g.inv_yres) : __ddiv_rn(d, g.yres);
 }
 
+using rzb::abs_ge_one;
 using rzb::ceil_clamp;
+using rzb::ceil_half_down;
 using rzb::f64_bits;
+using rzb::floor_half_up;
 using rzb::floor_clamp;
 using rzb::half_int;
 using rzb::nan_bits;
 
 // `(y - 0.5).ceil() as usize`, clamped to [0, nrows] (edges.rs:32-33).
-__device__ __forceinline__ int row_ceil(double py, int nrows) { return ceil_clamp(__dsub_rn(py, 0.5), nrows); }
+__device__ __forceinline__ int row_ceil(double py, int nrows) { return ceil_half_down(py, nrows); }
 
 // Rust f64::min / f64::max (NaN-ignoring)
 __device__ __forceinline__ double min_rs(double a, double b) {

@@ -342,6 +342,8 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   gr.pow2_y = is_pow2(info->yres);
   gr.inv_xres = gr.pow2_x ? 1.0 / info->xres : 0.0;
   gr.inv_yres = gr.pow2_y ? 1.0 / info->yres : 0.0;
+  gr.unit_x = info->xres == 1.0;
+  gr.unit_y = info->yres == 1.0;
   gr.nrows = (int)nrows;
   gr.ncols = (int)ncols;
   gr.ntx = ntx;

@@ -50,6 +50,12 @@ template <typename T> __device__ __forceinline__ T from_bits(unsigned long long 
   return v;
 }
 
+template <typename T> inline T from_bits_host(unsigned long long b) {
+  T v;
+  memcpy(&v, &b, sizeof(T));
+  return v;
+}
+
 enum { F_SUM = 0, F_FIRST = 1, F_LAST = 2, F_MIN = 3, F_MAX = 4, F_COUNT = 5, F_ANY = 6 };
 
 template <typename T, int FN>
@@ -104,6 +110,16 @@ template <typename T, int FN>
 __device__ __forceinline__ void apply_one(T& cur, T v, T bg, const BgF64& bgc) {
   if constexpr (std::is_same<T, double>::value) apply_px_f64<FN>(cur, v, bgc);
   else apply_px<T, FN>(cur, v, bg);
+}
+
+// The first write onto the background always takes the reset branch of
+// every pixel function (cur == bg, or cur is NaN when bg is NaN): its result
+// is the value itself, or 1 for count / any.  No arithmetic is issued, so
+// the compiler cannot speculate an FP64 add for it.
+template <typename T, int FN>
+__device__ __forceinline__ T first_write(T v) {
+  if constexpr (FN == F_COUNT || FN == F_ANY) return T(1);
+  else return v;
 }
 
 template <typename T>
@@ -194,7 +210,7 @@ constexpr int PX_WARPS = 4;
 
 template <typename T>
 constexpr int px_warp_bytes() {
-  return SMALL_MAX * 8 + ((SMALL_MAX * (int)sizeof(T) + 15) / 16) * 16 + TW * 2 + TW * PX_K + SMALL_MAX;
+  return SMALL_MAX * 8 + ((SMALL_MAX * (int)sizeof(T) + 15) / 16) * 16 + TW * 2 + TW * PX_K + SMALL_MAX + TW * 4;
 }
 
 template <typename T>
@@ -231,6 +247,7 @@ __global__ void __launch_bounds__(PX_WARPS * 32) k_fill_small(FillArgs a) {
   unsigned* depth = reinterpret_cast<unsigned*>(base + SMALL_MAX * 8 + ((SMALL_MAX * (int)sizeof(T) + 15) / 16) * 16);
   unsigned char* lists = reinterpret_cast<unsigned char*>(depth + TW / 2);
   unsigned char* longs = lists + TW * PX_K;
+  unsigned short* deep = reinterpret_cast<unsigned short*>(longs + SMALL_MAX);
   const T bg = from_bits<T>(a.bg);
   const BgF64 bgc = bg_f64(a.bg);
   T* out = static_cast<T*>(a.out);
@@ -238,10 +255,10 @@ __global__ void __launch_bounds__(PX_WARPS * 32) k_fill_small(FillArgs a) {
   for (unsigned long long b = (unsigned long long)blockIdx.x * PX_WARPS + warp; b < a.nbuckets; b += nwarps) {
     const unsigned o0 = a.offsets[b];
     const int n = (int)(a.offsets[b + 1] - o0);
-    const unsigned long long rowid = b / a.ntx;
-    const int c0 = (int)(b - rowid * a.ntx) << TW_SHIFT;
+    const unsigned rowid = (unsigned)b / a.ntx;  // 32-bit: a 64-bit divide runs on the FP64 pipe
+    const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
     const int len = min(TW, a.ncols - c0);
-    T* dst = out + rowid * (unsigned long long)a.ncols + c0;
+    T* dst = out + (unsigned long long)rowid * (unsigned long long)a.ncols + c0;
     if (n == 0) {
       store_bg<T>(dst, len, a.bg16, bg, lane, 32);
       continue;
@@ -257,28 +274,37 @@ __global__ void __launch_bounds__(PX_WARPS * 32) k_fill_small(FillArgs a) {
     }
     for (int i = lane; i < TW / 2; i += 32) depth[i] = 0u;
     __syncwarp();
+    // coverage: pixel writes are dealt to lanes with a warp prefix sum over
+    // the span lengths (every lane registers one pixel per step)
     bool over = false;
-    int nlong = 0;
     for (int i0 = 0; i0 < n; i0 += 32) {
       const int i = i0 + lane;
-      bool lng = false;
+      int x0 = 0, ln = 0;
       if (i < n) {
         const unsigned xs = sp[i].y;
-        const int x0 = (int)(xs & X_MASK), x1 = (int)((xs >> 12) & X_MASK);
-        if (x1 - x0 > PX_LONG) lng = true;
-        else
-          for (int x = x0; x < x1; ++x) over |= px_add(depth, lists, x, i);
+        x0 = (int)(xs & X_MASK);
+        ln = (int)((xs >> 12) & X_MASK) - x0;
       }
-      const unsigned m = __ballot_sync(0xFFFFFFFFu, lng);
-      if (lng) longs[nlong + __popc(m & ((1u << lane) - 1u))] = (unsigned char)i;
-      nlong += __popc(m);
-    }
-    __syncwarp();
-    for (int j = 0; j < nlong; ++j) {
-      const int i = longs[j];
-      const unsigned xs = sp[i].y;
-      const int x0 = (int)(xs & X_MASK), x1 = (int)((xs >> 12) & X_MASK);
-      for (int x = x0 + lane; x < x1; x += 32) over |= px_add(depth, lists, x, i);
+      int incl = ln;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+      const int excl = incl - ln;
+      for (int m0 = 0; m0 < total; m0 += 32) {
+        const int m = m0 + lane;
+        int s = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int e = __shfl_sync(0xFFFFFFFFu, excl, s + step);
+          if (e <= m) s += step;
+        }
+        const int es = __shfl_sync(0xFFFFFFFFu, excl, s);
+        const int xs0 = __shfl_sync(0xFFFFFFFFu, x0, s);
+        if (m < total) over |= px_add(depth, lists, xs0 + (m - es), i0 + s);
+      }
     }
     if (__any_sync(0xFFFFFFFFu, over)) {
       if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
@@ -286,41 +312,166 @@ __global__ void __launch_bounds__(PX_WARPS * 32) k_fill_small(FillArgs a) {
       continue;
     }
     __syncwarp();
-    for (int x = lane; x < len; x += 32) {
+    // pixels covered at most once are resolved in place; deeper ones are
+    // queued: depth-2 pixels (most of them) are folded in one dense pass,
+    // deeper ones go through a second queue and the general sorted fold, so
+    // the FP64 adds of a float sum run with dense lanes
+    int ndeep = 0;
+    for (int x0 = 0; x0 < len; x0 += 32) {
+      const int x = x0 + lane;
+      unsigned d = 0;
+      if (x < len) d = (depth[x >> 1] >> ((x & 1) * 16)) & 0xFFFFu;
+      const bool dp = d >= 2;
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, dp);
+      if (dp) deep[ndeep + __popc(m & ((1u << lane) - 1u))] = (unsigned short)x;
+      ndeep += __popc(m);
+      if (x < len && !dp) dst[x] = d == 1 ? first_write<T, FN>(vals[lists[x * PX_K]]) : bg;
+    }
+    __syncwarp();
+    int nd3 = 0;
+    unsigned short* deep3 = deep + TW;  // second queue, after the first
+    for (int q0 = 0; q0 < ndeep; q0 += 32) {
+      const int q = q0 + lane;
+      int x = 0;
+      unsigned d = 0;
+      if (q < ndeep) {
+        x = deep[q];
+        d = (depth[x >> 1] >> ((x & 1) * 16)) & 0xFFFFu;
+      }
+      const bool d3 = d >= 3;
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, d3);
+      if (d3) deep3[nd3 + __popc(m & ((1u << lane) - 1u))] = (unsigned short)x;
+      nd3 += __popc(m);
+      if (d == 2) {
+        // two spans in part order (the same part twice is a line; with the
+        // PixelCache it counts once)
+        unsigned i0 = lists[x * PX_K], i1 = lists[x * PX_K + 1];
+        unsigned p0 = sp[i0].x, p1 = sp[i1].x;
+        if (p1 < p0 || (p1 == p0 && i1 < i0)) {
+          const unsigned ti = i0; i0 = i1; i1 = ti;
+          const unsigned tp = p0; p0 = p1; p1 = tp;
+        }
+        T cur = first_write<T, FN>(vals[i0]);
+        if (!(DEDUP && p1 == p0 && (sp[i1].y & DEDUP_BIT))) apply_one<T, FN>(cur, vals[i1], bg, bgc);
+        dst[x] = cur;
+      }
+    }
+    __syncwarp();
+    for (int q = lane; q < nd3; q += 32) {
+      const int x = deep3[q];
       const unsigned d = (depth[x >> 1] >> ((x & 1) * 16)) & 0xFFFFu;
-      T cur = bg;
-      if (d) {
-        const uint2 pk = *reinterpret_cast<const uint2*>(lists + x * PX_K);
-        unsigned long long k[PX_K];
+      const uint2 pk = *reinterpret_cast<const uint2*>(lists + x * PX_K);
+      unsigned long long k[PX_K];
 #pragma unroll
-        for (int j = 0; j < PX_K; ++j) {
-          const unsigned idx = ((j < 4 ? pk.x : pk.y) >> (8 * (j & 3))) & 0xFFu;
-          k[j] = (unsigned)j < d ? (((unsigned long long)sp[idx].x << 32) | idx) : ~0ull;
-        }
-        // sort by (part, span index): 4-key network, or Batcher's 8-key
-        // odd-even merge network when more than 4 spans cover the pixel
-        if (d <= 4) {
-          cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[1], k[2]);
-        } else {
-          cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[4], k[5]); cswap(k[6], k[7]);
-          cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[4], k[6]); cswap(k[5], k[7]);
-          cswap(k[1], k[2]); cswap(k[5], k[6]);
-          cswap(k[0], k[4]); cswap(k[1], k[5]); cswap(k[2], k[6]); cswap(k[3], k[7]);
-          cswap(k[2], k[4]); cswap(k[3], k[5]);
-          cswap(k[1], k[2]); cswap(k[3], k[4]); cswap(k[5], k[6]);
-        }
-        unsigned prev = 0xFFFFFFFFu;
-#pragma unroll
-        for (int j = 0; j < PX_K; ++j) {
-          if ((unsigned)j < d) {
-            const unsigned idx = (unsigned)k[j] & 0xFFu, part = (unsigned)(k[j] >> 32);
-            if (DEDUP && (sp[idx].y & DEDUP_BIT) && part == prev) continue;  // PixelCache
-            prev = part;
-            apply_one<T, FN>(cur, vals[idx], bg, bgc);
-          }
-        }
+      for (int j = 0; j < PX_K; ++j) {
+        const unsigned idx = ((j < 4 ? pk.x : pk.y) >> (8 * (j & 3))) & 0xFFu;
+        k[j] = (unsigned)j < d ? (((unsigned long long)sp[idx].x << 32) | idx) : ~0ull;
+      }
+      // sort by (part, span index): 4-key network, or Batcher's 8-key
+      // odd-even merge network when more than 4 spans cover the pixel
+      if (d <= 4) {
+        cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[1], k[2]);
+      } else {
+        cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[4], k[5]); cswap(k[6], k[7]);
+        cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[4], k[6]); cswap(k[5], k[7]);
+        cswap(k[1], k[2]); cswap(k[5], k[6]);
+        cswap(k[0], k[4]); cswap(k[1], k[5]); cswap(k[2], k[6]); cswap(k[3], k[7]);
+        cswap(k[2], k[4]); cswap(k[3], k[5]);
+        cswap(k[1], k[2]); cswap(k[3], k[4]); cswap(k[5], k[6]);
+      }
+      unsigned prev = (unsigned)(k[0] >> 32);
+      T cur = first_write<T, FN>(vals[(unsigned)k[0] & 0xFFu]);
+      for (unsigned j = 1; j < d; ++j) {
+        const unsigned long long kj = j < 4 ? (j < 2 ? k[1] : (j == 2 ? k[2] : k[3]))
+                                           : (j < 6 ? (j == 4 ? k[4] : k[5]) : (j == 6 ? k[6] : k[7]));
+        const unsigned idx = (unsigned)kj & 0xFFu, part = (unsigned)(kj >> 32);
+        if (DEDUP && (sp[idx].y & DEDUP_BIT) && part == prev) continue;  // PixelCache
+        prev = part;
+        apply_one<T, FN>(cur, vals[idx], bg, bgc);
       }
       dst[x] = cur;
+    }
+    __syncwarp();
+  }
+}
+
+// ---- order-free fill: count / any --------------------------------------
+// Integer `count` with background 0 (and float count with background 0 or
+// NaN) equals the pixel's coverage depth: every write after the first adds
+// one and no intermediate count can equal the background.  `any` is 1
+// wherever the depth is non-zero.  Neither needs values, lists or order.
+constexpr int DEPTH_WARPS = 8;
+constexpr int DEPTH_MAX_SPANS = 65535;  // 16-bit depth counters
+
+template <typename T, int FN>
+__global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
+  __shared__ unsigned s_depth[DEPTH_WARPS][TW / 2];
+  const Ctrl* ctrl = a.ctrl;
+  if (ctrl->err || ctrl->span_count > a.span_cap) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned* depth = s_depth[warp];
+  const T bg = from_bits<T>(a.bg);
+  T* out = static_cast<T*>(a.out);
+  const unsigned long long nwarps = (unsigned long long)gridDim.x * DEPTH_WARPS;
+  for (unsigned long long b = (unsigned long long)blockIdx.x * DEPTH_WARPS + warp; b < a.nbuckets; b += nwarps) {
+    const unsigned o0 = a.offsets[b];
+    const int n = (int)(a.offsets[b + 1] - o0);
+    const unsigned rowid = (unsigned)b / a.ntx;
+    const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
+    const int len = min(TW, a.ncols - c0);
+    T* dst = out + (unsigned long long)rowid * (unsigned long long)a.ncols + c0;
+    if (n == 0) {
+      store_bg<T>(dst, len, a.bg16, bg, lane, 32);
+      continue;
+    }
+    if (n > DEPTH_MAX_SPANS) {
+      if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
+      continue;
+    }
+    for (int i = lane; i < TW / 2; i += 32) depth[i] = 0u;
+    __syncwarp();
+    for (int i0 = 0; i0 < n; i0 += 32) {
+      const int i = i0 + lane;
+      int x0 = 0, ln = 0;
+      if (i < n) {
+        const unsigned xs = a.spans[o0 + i].y;
+        x0 = (int)(xs & X_MASK);
+        ln = (int)((xs >> 12) & X_MASK) - x0;
+      }
+      int incl = ln;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+      const int excl = incl - ln;
+      for (int m0 = 0; m0 < total; m0 += 32) {
+        const int m = m0 + lane;
+        int s = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int e = __shfl_sync(0xFFFFFFFFu, excl, s + step);
+          if (e <= m) s += step;
+        }
+        const int es = __shfl_sync(0xFFFFFFFFu, excl, s);
+        const int xs0 = __shfl_sync(0xFFFFFFFFu, x0, s);
+        if (m < total) {
+          const int x = xs0 + (m - es);
+          atomicAdd(&depth[x >> 1], 1u << ((x & 1) * 16));
+        }
+      }
+    }
+    __syncwarp();
+    for (int x = lane; x < len; x += 32) {
+      const unsigned d = (depth[x >> 1] >> ((x & 1) * 16)) & 0xFFFFu;
+      T v = bg;
+      if (d) {
+        if constexpr (FN == F_ANY) v = T(1);
+        else if constexpr (std::is_integral<T>::value) v = (T)(typename std::make_unsigned<T>::type)d;
+        else v = (T)d;
+      }
+      dst[x] = v;
     }
     __syncwarp();
   }
@@ -384,7 +535,7 @@ __global__ void __launch_bounds__(BIG_THREADS) k_fill_big(FillArgs a) {
     const unsigned long long b = a.big[bi];
     const unsigned o0 = a.offsets[b];
     const int n = (int)(a.offsets[b + 1] - o0);
-    const unsigned long long rowid = b / a.ntx;
+    const unsigned long long rowid = (unsigned)b / a.ntx;
     const int c0 = (int)(b - rowid * a.ntx) << TW_SHIFT;
     const int len = min(TW, a.ncols - c0);
     T* dst = out + rowid * (unsigned long long)a.ncols + c0;
@@ -495,8 +646,34 @@ __global__ void __launch_bounds__(BIG_THREADS) k_fill_big(FillArgs a) {
 
 // Host launcher shared by the per-dtype translation units.
 template <typename T>
+bool depth_exact(const FillArgs& a, int fn, bool dedup) {
+  if (fn == F_ANY) return true;
+  if (fn != F_COUNT || dedup) return false;
+  const T bg = from_bits_host<T>(a.bg);
+  if constexpr (std::is_integral<T>::value) return bg == T(0);
+  else return bg == T(0) || bg != bg;
+}
+
+template <typename T>
 int launch_fill_t(const FillArgs& a, int fn, bool dedup, int num_sms, cudaStream_t s) {
   int launches = 0;
+  if (depth_exact<T>(a, fn, dedup)) {
+    unsigned long long want = (a.nbuckets + DEPTH_WARPS - 1) / DEPTH_WARPS;
+    unsigned grid = (unsigned)(want < (unsigned long long)num_sms * 16 ? want : num_sms * 16ull);
+    if (grid == 0) grid = 1;
+    if (fn == F_ANY) {
+      k_fill_depth<T, F_ANY><<<grid, DEPTH_WARPS * 32, 0, s>>>(a);
+      cudaFuncSetAttribute(k_fill_big<T, F_ANY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           big_smem_bytes<T, false>());
+      k_fill_big<T, F_ANY, false><<<num_sms * 2, BIG_THREADS, big_smem_bytes<T, false>(), s>>>(a);
+    } else {
+      k_fill_depth<T, F_COUNT><<<grid, DEPTH_WARPS * 32, 0, s>>>(a);
+      cudaFuncSetAttribute(k_fill_big<T, F_COUNT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           big_smem_bytes<T, false>());
+      k_fill_big<T, F_COUNT, false><<<num_sms * 2, BIG_THREADS, big_smem_bytes<T, false>(), s>>>(a);
+    }
+    return 2;
+  }
 #define RZ_FILL_CASE(FNV, DD)                                                                        \
   {                                                                                                  \
     constexpr int ss = small_smem_bytes<T>();                                                        \

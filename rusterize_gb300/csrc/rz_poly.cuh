@@ -64,11 +64,15 @@ __device__ __forceinline__ void poly_flush(const Geo& geo, const Grid& g, const 
     const unsigned vv = q.v[i];
     const bool top0 = vv >> 31;
     const unsigned long long v = vs + (vv & 0x7FFFFFFFu);
-    // extract_ring's horizontal filter (edges.rs:100): |y0 - y1| >= EPSILON
-    const unsigned long long dbits = f64_bits(__dsub_rn(py0, py1)) & 0x7FFFFFFFFFFFFFFFull;
-    if (!(dbits >= 0x3CB0000000000000ull && dbits <= 0x7FF0000000000000ull)) {
-      q.rows[i] &= 0xFFu;  // no crossings
-      continue;
+    // extract_ring's horizontal filter (edges.rs:100): |y0 - y1| >= EPSILON.
+    // Queued end points differ; two distinct doubles of magnitude >= 1 are
+    // at least 2^-52 apart, so only smaller ones need the subtraction.
+    if (!(abs_ge_one(py0) && abs_ge_one(py1))) {
+      const unsigned long long dbits = f64_bits(__dsub_rn(py0, py1)) & 0x7FFFFFFFFFFFFFFFull;
+      if (!(dbits >= 0x3CB0000000000000ull && dbits <= 0x7FF0000000000000ull)) {
+        q.rows[i] &= 0xFFu;  // no crossings
+        continue;
+      }
     }
     const double px0 = to_px(g, geo.xy[v].x), px1 = to_px(g, geo.xy[v + 1].x);
     const double xt = top0 ? px0 : px1, yt = top0 ? py0 : py1;
@@ -115,7 +119,7 @@ __device__ __forceinline__ void poly_flush(const Geo& geo, const Grid& g, const 
         if (!(xb >> 63)) continue;  // +NaN: after every number, pairs into an empty span
         r = 0;
       } else {
-        r = floor_clamp(__dadd_rn(x, 0.5), g.ncols);  // burners.rs:310-311
+        r = floor_half_up(x, g.ncols);  // floor(x + 0.5) clamped, burners.rs:310-311
       }
       const int loc = r - w.col0;
       if (loc < 0 || loc >= w.nbits) {
@@ -373,6 +377,99 @@ __device__ __forceinline__ void extract_spans(const unsigned* bm, const PolyWin&
   }
 }
 
+// Narrow parts (one warp per window): a row has at most SMALL_BW words, so
+// one LANE walks a whole row; the per-row piece offsets come from one warp
+// scan per 32 rows.
+__device__ __forceinline__ unsigned lane_row_pieces(const unsigned* row, int bw, int col0) {
+  unsigned par = 0, pieces = 0;
+  int start = 0;
+  for (int wd = 0; wd < bw; ++wd) {
+    unsigned bits = row[wd];
+    while (bits) {
+      const int pos = wd * 32 + __ffs(bits) - 1;
+      bits &= bits - 1;
+      if (par) {
+        const int xs = col0 + start, xe = col0 + pos;
+        pieces += (unsigned)(((xe - 1) >> TW_SHIFT) - (xs >> TW_SHIFT) + 1);
+      } else {
+        start = pos;
+      }
+      par ^= 1u;
+    }
+  }
+  return pieces;
+}
+
+__device__ __forceinline__ void find_odd_rows_lane(const unsigned* bm, int nr, int bw, int* rowslot, int* oddrow,
+                                                   int* oddmax, int* s_nodd) {
+  const int lane = threadIdx.x & 31;
+  for (int i = lane; i < nr; i += 32) {
+    unsigned par = 0;
+    for (int wd = 0; wd < bw; ++wd) par ^= (unsigned)__popc(bm[i * bw + wd]);
+    if (par & 1u) {
+      const int slot = atomicAdd(s_nodd, 1);
+      rowslot[i] = slot;
+      oddrow[slot] = i;
+      oddmax[slot] = -1;
+    }
+  }
+}
+
+__device__ __forceinline__ void extract_spans_lane(const unsigned* bm, const PolyWin& w, const PartPlan& pl,
+                                                   unsigned long long p, const Grid& g, const SpanBuf& sb,
+                                                   unsigned* bucket_count, Ctrl* ctrl, unsigned long long& npix) {
+  const int lane = threadIdx.x & 31;
+  const int nr = w.r1 - w.r0, bw = w.bw;
+  // pieces of rows lane and lane + 32, their exclusive offsets, one reservation
+  const unsigned c0 = lane < nr ? lane_row_pieces(bm + lane * bw, bw, pl.col0) : 0u;
+  const unsigned c1 = lane + 32 < nr ? lane_row_pieces(bm + (lane + 32) * bw, bw, pl.col0) : 0u;
+  unsigned i0 = c0, i1 = c1;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t0 = __shfl_up_sync(0xFFFFFFFFu, i0, o), t1 = __shfl_up_sync(0xFFFFFFFFu, i1, o);
+    if (lane >= o) { i0 += t0; i1 += t1; }
+  }
+  const unsigned tot0 = __shfl_sync(0xFFFFFFFFu, i0, 31);
+  const unsigned tot = tot0 + __shfl_sync(0xFFFFFFFFu, i1, 31);
+  unsigned long long base = 0;
+  if (lane == 0 && tot) base = atomicAdd(&ctrl->span_count, (unsigned long long)tot);
+  base = __shfl_sync(0xFFFFFFFFu, base, 0);
+  const unsigned long long rowband = (unsigned long long)pl.band * (unsigned)g.nrows;
+  for (int h = 0; h < 2; ++h) {
+    const int i = lane + 32 * h;
+    if (i >= nr) continue;
+    unsigned long long slot = base + (h == 0 ? i0 - c0 : tot0 + i1 - c1);
+    const unsigned long long rowid = rowband + (unsigned)(w.r0 + i);
+    const unsigned* row = bm + i * bw;
+    unsigned par = 0;
+    int start = 0;
+    for (int wd = 0; wd < bw; ++wd) {
+      unsigned bits = row[wd];
+      while (bits) {
+        const int pos = wd * 32 + __ffs(bits) - 1;
+        bits &= bits - 1;
+        if (par) {
+          const int xs = pl.col0 + start, xe = pl.col0 + pos;
+          npix += (unsigned long long)(xe - xs);
+          for (int t = xs >> TW_SHIFT; (t << TW_SHIFT) < xe; ++t, ++slot) {
+            const int tb = t << TW_SHIFT;
+            const unsigned a = (unsigned)(max(xs, tb) - tb), b = (unsigned)(min(xe, tb + TW) - tb);
+            const unsigned bucket = (unsigned)(rowid * g.ntx + (unsigned)t);
+            if (slot < sb.cap) {
+              sb.bucket[slot] = bucket;
+              sb.part[slot] = (unsigned)p;
+              sb.xs[slot] = a | (b << 12);
+            }
+            atomicAdd(&bucket_count[bucket], 1u);
+          }
+        } else {
+          start = pos;
+        }
+        par ^= 1u;
+      }
+    }
+  }
+}
+
 // one (part, window): zero the bitmap, toggle crossings, fix odd rows, emit
 template <int NT, int QCAP>
 __device__ __forceinline__ void poly_window(const Geo& geo, const Grid& g, const PartPlan& pl, unsigned long long p,
@@ -394,7 +491,8 @@ __device__ __forceinline__ void poly_window(const Geo& geo, const Grid& g, const
   scope_sync<NT>();
   const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
   poly_pass<0, NT, QCAP>(geo, g, rb, re, win, bm, q, s_q, rowslot, oddmax, ctrl, p, ncross);
-  find_odd_rows<NT>(bm, nr, bw, rowslot, oddrow, oddmax, s_nodd);
+  if constexpr (NT == 32) find_odd_rows_lane(bm, nr, bw, rowslot, oddrow, oddmax, s_nodd);
+  else find_odd_rows<NT>(bm, nr, bw, rowslot, oddrow, oddmax, s_nodd);
   scope_sync<NT>();
   if (*s_nodd > 0) {
     unsigned long long dummy = 0;
@@ -406,7 +504,8 @@ __device__ __forceinline__ void poly_window(const Geo& geo, const Grid& g, const
     scope_sync<NT>();
   }
   // oddrow is free again: it holds the per-row piece offsets
-  extract_spans<NT>(bm, win, pl, p, g, sb, bucket_count, ctrl, npix, reinterpret_cast<unsigned*>(oddrow), s_base);
+  if constexpr (NT == 32) extract_spans_lane(bm, win, pl, p, g, sb, bucket_count, ctrl, npix);
+  else extract_spans<NT>(bm, win, pl, p, g, sb, bucket_count, ctrl, npix, reinterpret_cast<unsigned*>(oddrow), s_base);
   scope_sync<NT>();
 }
 

@@ -63,6 +63,39 @@ int main() {
   }
   const int big[] = {2147483646, 2147483647, 1 << 30, (1 << 30) + 1};
   for (int y : big) { ++n; if (rzb::half_int(y) != (double)y + 0.5) ++bad; }
+  // the +-0.5 roundings used by the scanline code
+  auto half_check = [&](double t) {
+    for (int hi : his) {
+      ++n;
+      if (!std::isnan(t) && rzb::floor_half_up(t, hi) != ref_floor_clamp(t + 0.5, hi)) {
+        if (bad < 5) printf("floor_half_up %.17g hi=%d\n", t, hi); ++bad;
+      }
+      if (rzb::ceil_half_down(t, hi) != ref_ceil_clamp(t - 0.5, hi)) {
+        if (bad < 5) printf("ceil_half_down %.17g hi=%d\n", t, hi); ++bad;
+      }
+    }
+  };
+  for (double t : specials) half_check(t);
+  for (int k = -60; k < 40; ++k) {           // every binade edge and its neighbours
+    double p = std::ldexp(1.0, k);
+    for (double c : {p, p - 0.5, p + 0.5, p - 1.0}) {
+      double v = c;
+      for (int j = 0; j < 6; ++j) { half_check(v); half_check(-v); v = std::nextafter(v, 0.0); }
+      v = c;
+      for (int j = 0; j < 6; ++j) { half_check(v); v = std::nextafter(v, 1e300); }
+    }
+  }
+  for (int i = 0; i < 2000000; ++i) {
+    uint64_t b = rng();
+    double t;
+    switch (i % 4) {
+      case 0: std::memcpy(&t, &b, 8); break;
+      case 1: t = (double)(int64_t)(b % 10000000) / 4096.0 - 100.0; break;
+      case 2: t = std::nextafter((double)(b % 50000) + 0.5, (i & 1) ? 1e9 : -1e9); break;
+      default: t = std::ldexp((double)(b >> 11), -(int)(b % 60)); break;
+    }
+    half_check(t);
+  }
   // f64 comparisons on bit patterns vs IEEE
   const double cmpv[] = {0.0, -0.0, 1.0, -1.0, 2.5, -2.5, 1e-310, -1e-310, INFINITY, -INFINITY, NAN, -NAN,
                          1e308, -1e308, 3.0, 0.1};
@@ -74,6 +107,7 @@ int main() {
     if (rzb::eq_bg_f64(ab, bg) != (a == b)) { if (bad < 5) printf("eq %.17g %.17g\n", a, b); ++bad; }
   };
   for (double a : cmpv) for (double b : cmpv) cmp_check(a, b);
+  for (double a : cmpv) { ++n; if (rzb::abs_ge_one(a) != (std::fabs(a) >= 1.0)) { if (bad < 5) printf("abs_ge_one %g\n", a); ++bad; } }
   for (int i = 0; i < 1000000; ++i) {
     uint64_t x = rng(), y = (i & 1) ? rng() : x ^ (rng() & 0xF);
     double a, b;
