@@ -196,6 +196,36 @@ rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void* values,
  * around calls or to order other work after them. */
 void* rz_context_stream(rz_context* ctx);
 
+/* Allocation-free burn.  No counterpart in the reference: it exists for
+ * callers that must not allocate device memory when they burn -- code that
+ * runs while a stream is being captured into a CUDA graph (cudaMalloc is not
+ * allowed there), serving loops whose memory is budgeted up front and must
+ * not grow or synchronise the device behind the caller's back, and plugin
+ * hosts that own every allocation.  Same arguments and results as
+ * rz_rasterize, except:
+ *   - no context: work goes to `stream` (a cudaStream_t, NULL = default);
+ *   - the geometry arrays, per-geometry values, band_of_geom and `out` are
+ *     DEVICE pointers (xy 16-byte aligned); a scalar value (with
+ *     RZ_FLAG_SCALAR_VALUE) and the background are host values;
+ *   - all scratch comes from one static device array of
+ *     RZ_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library
+ *     until the process exits; a job whose tables, buckets or spans do not
+ *     fit is rejected with RZ_VALUE_ERROR and a message giving the limit;
+ *   - the first call on a device resolves that array's address (once per
+ *     device, with the device current); make that first call before any
+ *     stream capture;
+ *   - all calls share the array and it keeps the last call's contents: each
+ *     call clears what must start at zero, and calls whose work overlaps on
+ *     the GPU race on it (serialise them on one stream);
+ *   - the call waits for its own work on `stream` before returning (it reads
+ *     back a small status block into host stack memory); no timings. */
+#define RZ_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const void* values,
+                               const void* background, const uint32_t* band_of_geom,
+                               uint32_t n_bands, const rz_raster_info* info, rz_pixel_fn fn,
+                               rz_dtype out_dtype, uint32_t flags, void* out, rz_stats* stats,
+                               char* err, size_t errlen);
+
 /* Block until all work queued on the context's stream has finished. */
 rz_status rz_context_synchronize(rz_context* ctx, char* err, size_t errlen);
 

@@ -27,6 +27,8 @@ FLAG_NO_TIMING = 1 << 4
 
 RI_SHAPE, RI_RES, RI_EXTENT, RI_TAP = 1, 2, 4, 8
 
+NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024  # RZ_NOALLOC_SCRATCH_BYTES
+
 # rz_dtype codes, in the order of python/src/rusterize.rs:171-182
 DTYPES = {
     "uint8": 0, "uint16": 1, "uint32": 2, "uint64": 3,
@@ -100,6 +102,9 @@ PROTOTYPES = {
     "rz_rasterize": (c_int, [c_void_p, POINTER(RzGeoms), c_void_p, c_void_p, c_void_p, c_uint32,
                              POINTER(RzRasterInfo), c_int, c_int, c_uint32, c_void_p, POINTER(RzStats),
                              c_char_p, c_size_t]),
+    "rz_rasterize_noalloc": (c_int, [c_void_p, POINTER(RzGeoms), c_void_p, c_void_p, c_void_p, c_uint32,
+                                     POINTER(RzRasterInfo), c_int, c_int, c_uint32, c_void_p, POINTER(RzStats),
+                                     c_char_p, c_size_t]),
 }
 
 _lib = None

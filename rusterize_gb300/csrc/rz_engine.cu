@@ -10,6 +10,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "rz_device.cuh"
 #include "rz_fill.cuh"
@@ -512,6 +513,274 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     }
     stats->ms_host_total =
         std::chrono::duration<float, std::milli>(clk::now() - t_host0).count();
+  }
+  return RZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free burn (rz_rasterize_noalloc).
+//
+// Some callers cannot allocate device memory at the moment they burn: code
+// running while a stream is being captured into a CUDA graph (cudaMalloc is
+// not allowed there), serving loops whose memory is budgeted up front and
+// must not grow or synchronise the device behind the caller's back, and
+// plugin hosts that own every allocation themselves.  This entry point runs
+// the same kernels as rz_rasterize, but every scratch buffer is carved out of
+// the file-scope array below instead of the context's growable arena.  The
+// array is RZ_NOALLOC_SCRATCH_BYTES large and is held by every GPU that loads
+// this library until the process exits.  All calls share it: it keeps the
+// last call's contents (everything that must start at zero is cleared by
+// each call), and calls whose work overlaps on the GPU race on it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[RZ_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+struct NoAllocDevice {
+  bool ready = false;
+  unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
+  int sms = 0, poly_bps = 1, narrow_bps = 1;
+};
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+NoAllocDevice g_noalloc[kNoAllocMaxDevices];
+
+}  // namespace
+
+extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const void* values,
+                                          const void* background, const uint32_t* band_of_geom, uint32_t n_bands,
+                                          const rz_raster_info* info, rz_pixel_fn fn, rz_dtype dt, uint32_t flags,
+                                          void* out, rz_stats* stats, char* err, size_t errlen) {
+  rz::clear_err(err, errlen);
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (!g || !info || !background || !out) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null argument");
+  const size_t tsize = rz_dtype_size(dt);
+  if (tsize == 0) return fail(err, errlen, RZ_VALUE_ERROR, "Unsupported dtype");
+  if ((int)fn < 0 || (int)fn > 6) return fail(err, errlen, RZ_VALUE_ERROR, "Unknown pixel function");
+  if (band_of_geom && n_bands == 0) return fail(err, errlen, RZ_INVALID_ARGUMENT, "n_bands must be > 0");
+  if (flags & RZ_FLAG_ALL_TOUCHED)
+    return fail(err, errlen, RZ_VALUE_ERROR, "all_touched is not implemented by the GB300 engine yet");
+  const unsigned long long nb = band_of_geom ? n_bands : 1;
+  if (info->nrows >= (1ull << 31) - 1 || info->ncols >= (1ull << 31) - 1)
+    return fail(err, errlen, RZ_VALUE_ERROR, "raster dimensions must be below 2^31-1");
+  const unsigned long long nrows = info->nrows, ncols = info->ncols;
+  const unsigned long long out_elems = nb * nrows * ncols;
+  const unsigned ntx = (unsigned)((ncols + TW - 1) >> TW_SHIFT);
+  const unsigned long long nbuckets = nb * nrows * ntx;
+  const unsigned long long G = g->n_geoms, P = g->n_parts, R = g->n_rings, V = g->n_vertices;
+  if (G >= 0xFFFFFFFFull || P >= 0xFFFFFFFFull || nbuckets >= 0xFFFFFFFFull)
+    return fail(err, errlen, RZ_VALUE_ERROR, "job too large for 32-bit part / bucket indices");
+  if (!g->part_offsets || !g->part_kind || !g->ring_offsets || !g->vertex_offsets || (V && !g->xy))
+    return fail(err, errlen, RZ_INVALID_ARGUMENT, "geometry table has null arrays");
+  if (reinterpret_cast<uintptr_t>(g->xy) & 15)
+    return fail(err, errlen, RZ_INVALID_ARGUMENT, "device xy must be 16-byte aligned");
+  unsigned long long bg_bits = 0, scalar_bits = one_bits(dt);
+  std::memcpy(&bg_bits, background, tsize);
+  const bool per_geom_values = values && !(flags & RZ_FLAG_SCALAR_VALUE);
+  if (values && (flags & RZ_FLAG_SCALAR_VALUE)) {
+    scalar_bits = 0;
+    std::memcpy(&scalar_bits, values, tsize);
+  }
+  if (stats) stats->out_bytes = out_elems * tsize;
+  if (out_elems == 0) return RZ_OK;
+
+  // scratch layout inside the static array (inputs and output are the caller's)
+  Layout L;
+  const size_t o_pg = L.take(4 * (P ? P : 1));
+  const size_t o_plan = L.take(sizeof(PartPlan) * (P ? P : 1));
+  const size_t o_cnt = L.take(8 * PC_N * (P ? P : 1));
+  const size_t o_poff = L.take(8 * PC_N * (P + 1));
+  const size_t o_tmp64 = L.take(8 * scan_temp_elems(P, PC_N));
+  const size_t o_last = L.take(8 * (P ? P : 1));
+  const size_t o_lp = L.take(4 * (P ? P : 1));
+  const size_t o_pp = L.take(4 * (P ? P : 1));
+  const size_t o_bc = L.take(4 * nbuckets);
+  const size_t o_boff = L.take(4 * (nbuckets + 1));
+  const size_t o_tmp32 = L.take(4 * scan_temp_elems(nbuckets, 1));
+  const size_t o_big = L.take(4 * nbuckets);
+  const size_t o_ctrl = L.take(sizeof(Ctrl));
+  const size_t o_spans = L.take(0);
+  const size_t min_spans = 1024;
+  if (o_spans + 20 * min_spans + 16 > RZ_NOALLOC_SCRATCH_BYTES)
+    return fail(err, errlen, RZ_VALUE_ERROR,
+                "job needs %zu bytes of scratch before any span; the allocation-free entry point is limited to "
+                "%zu bytes (use rz_rasterize)",
+                o_spans + 20 * min_spans + 16, (size_t)RZ_NOALLOC_SCRATCH_BYTES);
+  unsigned long long cap = ((RZ_NOALLOC_SCRATCH_BYTES - o_spans - 16) / 20) & ~1ull;
+  if (cap > 0xFFFFFFF0ull) cap = 0xFFFFFFF0ull;
+
+  int dev = 0;
+  RZ_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(err, errlen, RZ_NO_DEVICE, "device %d unsupported", dev);
+  NoAllocDevice nd;
+  {
+    // one-time set-up per device, with that device current: resolve the
+    // array's device address (host code cannot use the symbol itself)
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoAllocDevice& d = g_noalloc[dev];
+    if (!d.ready) {
+      void* p = nullptr;
+      RZ_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      RZ_CUDA(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
+      RZ_CUDA(cudaFuncSetAttribute(k_poly_spans, cudaFuncAttributeMaxDynamicSharedMemorySize, POLY_SMEM));
+      RZ_CUDA(cudaFuncSetAttribute(k_poly_spans_narrow, cudaFuncAttributeMaxDynamicSharedMemorySize, SMALL_SMEM));
+      RZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.poly_bps, k_poly_spans, POLY_THREADS, POLY_SMEM));
+      RZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.narrow_bps, k_poly_spans_narrow, SMALL_WARPS * 32,
+                                                            SMALL_SMEM));
+      if (d.poly_bps < 1) d.poly_bps = 1;
+      if (d.narrow_bps < 1) d.narrow_bps = 1;
+      d.scratch = static_cast<unsigned char*>(p);
+      d.ready = true;
+    }
+    nd = d;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned char* mb = nd.scratch;
+  auto at = [&](size_t o) { return static_cast<void*>(mb + o); };
+
+  Geo geo;
+  geo.n_geoms = G;
+  geo.n_parts = P;
+  geo.n_rings = R;
+  geo.n_vertices = V;
+  geo.part_offsets = reinterpret_cast<const unsigned long long*>(g->part_offsets);
+  geo.part_kind = g->part_kind;
+  geo.ring_offsets = reinterpret_cast<const unsigned long long*>(g->ring_offsets);
+  geo.vertex_offsets = reinterpret_cast<const unsigned long long*>(g->vertex_offsets);
+  geo.xy = reinterpret_cast<const double2*>(g->xy);
+  geo.bands = band_of_geom;
+
+  Grid gr;
+  gr.xmin = info->xmin;
+  gr.ymax = info->ymax;
+  gr.xres = info->xres;
+  gr.yres = info->yres;
+  gr.pow2_x = is_pow2(info->xres);
+  gr.pow2_y = is_pow2(info->yres);
+  gr.inv_xres = gr.pow2_x ? 1.0 / info->xres : 0.0;
+  gr.inv_yres = gr.pow2_y ? 1.0 / info->yres : 0.0;
+  gr.unit_x = info->xres == 1.0;
+  gr.unit_y = info->yres == 1.0;
+  gr.nrows = (int)nrows;
+  gr.ncols = (int)ncols;
+  gr.ntx = ntx;
+  gr.n_bands = (unsigned)nb;
+  const bool dedup = info->xres != info->yres && (fn == RZ_SUM || fn == RZ_COUNT);
+
+  Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
+  unsigned* part_geom = static_cast<unsigned*>(at(o_pg));
+  PartPlan* plan = static_cast<PartPlan*>(at(o_plan));
+  unsigned long long* counts = static_cast<unsigned long long*>(at(o_cnt));
+  unsigned long long* poff = static_cast<unsigned long long*>(at(o_poff));
+  unsigned long long* last_kept = static_cast<unsigned long long*>(at(o_last));
+  unsigned* line_parts = static_cast<unsigned*>(at(o_lp));
+  unsigned* point_parts = static_cast<unsigned*>(at(o_pp));
+  unsigned* bcount = static_cast<unsigned*>(at(o_bc));
+  unsigned* boff = static_cast<unsigned*>(at(o_boff));
+  unsigned* big = static_cast<unsigned*>(at(o_big));
+  const int sms = nd.sms;
+  int launches = 0;
+
+  RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
+  const unsigned long long maxn = std::max({G + 1, P + 1, R + 1});
+  k_validate<<<grid_for(maxn, 256, sms * 8), 256, 0, s>>>(geo, d_ctrl);
+  ++launches;
+  if (band_of_geom && G) {
+    k_check_bands<<<grid_for(G, 256, sms * 8), 256, 0, s>>>(geo, (unsigned)nb, d_ctrl);
+    ++launches;
+  }
+  if (G) {
+    k_part_geom<<<grid_for(G, 256, sms * 16), 256, 0, s>>>(geo, part_geom, d_ctrl);
+    ++launches;
+  }
+  if (P) {
+    k_part_prep<<<grid_for(P, 8, sms * 32), 256, 0, s>>>(geo, gr, part_geom, plan, counts, d_ctrl);
+    ++launches;
+  }
+  launches += scan<unsigned long long, PC_N>(counts, poff, P, static_cast<unsigned long long*>(at(o_tmp64)), s);
+  if (P) {
+    k_part_lists<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(geo, poff, line_parts, point_parts, d_ctrl);
+    ++launches;
+  }
+  RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
+  SpanBuf sb;
+  sb.cap = cap;
+  sb.bucket = static_cast<unsigned*>(at(o_spans));
+  sb.part = sb.bucket + cap;
+  sb.xs = sb.part + cap;
+  uint2* sorted = reinterpret_cast<uint2*>(sb.xs + cap);
+  k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
+  RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
+  ++launches;
+  if (P) {
+    k_poly_spans_narrow<<<sms * nd.narrow_bps, SMALL_WARPS * 32, SMALL_SMEM, s>>>(geo, gr, plan, poff, sb, bcount,
+                                                                                   d_ctrl);
+    k_poly_spans<<<sms * nd.poly_bps, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, plan, poff, sb, bcount, d_ctrl);
+    k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept, dedup ? DEDUP_BIT : 0u, sb,
+                                         bcount, d_ctrl);
+    k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
+                                                             dedup ? DEDUP_BIT : 0u, sb, bcount, d_ctrl);
+    k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, point_parts, sb, bcount, d_ctrl);
+    launches += 5;
+  }
+  launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
+  k_scatter<<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, d_ctrl);
+  ++launches;
+  FillArgs fa;
+  fa.offsets = boff;
+  fa.spans = sorted;
+  fa.nbuckets = nbuckets;
+  fa.values = per_geom_values ? values : nullptr;
+  fa.scalar = scalar_bits;
+  fa.part_geom = part_geom;
+  fa.out = out;
+  fa.bg = bg_bits;
+  {
+    unsigned char pat[16];
+    for (int i = 0; i < 16; i += (int)tsize) std::memcpy(pat + i, &bg_bits, tsize);
+    std::memcpy(&fa.bg16, pat, 16);
+  }
+  fa.nrows = (int)nrows;
+  fa.ncols = (int)ncols;
+  fa.ntx = ntx;
+  fa.big = big;
+  fa.ctrl = d_ctrl;
+  fa.span_cap = cap;
+  launches += fill_for(dt)(fa, (int)fn, dedup, sms, s);
+  RZ_CUDA(cudaGetLastError());
+  Ctrl hc;  // the caller's stack, no pinned buffer
+  RZ_CUDA(cudaMemcpyAsync(&hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+  RZ_CUDA(cudaStreamSynchronize(s));
+  if (hc.err) {
+    const unsigned long long ix = hc.err_index;
+    switch (hc.err) {
+      case ERR_BAD_TABLE:
+        return fail(err, errlen, RZ_INVALID_ARGUMENT, "geometry table is inconsistent (%s offsets, index %llu)",
+                    (ix >> 62) == 0 ? "part" : ((ix >> 62) == 1 ? "ring" : "vertex"), ix & ((1ull << 62) - 1));
+      case ERR_BAD_KIND: return fail(err, errlen, RZ_INVALID_ARGUMENT, "invalid part kind at part %llu", ix);
+      case ERR_BAD_BAND: return fail(err, errlen, RZ_INVALID_ARGUMENT, "band index out of range at geometry %llu", ix);
+      case ERR_BITMAP:
+        return fail(err, errlen, RZ_RUNTIME_ERROR, "polygon part %llu has non-finite or out-of-range coordinates", ix);
+      case ERR_TOO_WIDE:
+        return fail(err, errlen, RZ_VALUE_ERROR, "polygon part %llu is wider than %d raster columns", ix,
+                    BITMAP_WORDS * 32 - 64);
+      case ERR_LINE_LONG:
+        return fail(err, errlen, RZ_VALUE_ERROR, "line segment at vertex %llu spans more than 2^26 pixels", ix);
+      default: return fail(err, errlen, RZ_RUNTIME_ERROR, "engine error %u", hc.err);
+    }
+  }
+  if (hc.span_count > cap)
+    return fail(err, errlen, RZ_VALUE_ERROR,
+                "job produced %llu spans; the allocation-free entry point holds at most %llu in its %zu-byte "
+                "scratch (use rz_rasterize)",
+                hc.span_count, cap, (size_t)RZ_NOALLOC_SCRATCH_BYTES);
+  if (stats) {
+    stats->edges = hc.edges;
+    stats->crossings = hc.crossings;
+    stats->spans = hc.span_count;
+    stats->pixel_writes = hc.pixel_writes;
+    stats->big_buckets = hc.big_count;
+    stats->buckets = nbuckets;
+    stats->kernel_launches = (uint32_t)launches;
   }
   return RZ_OK;
 }
