@@ -197,11 +197,11 @@ rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void* values,
 void* rz_context_stream(rz_context* ctx);
 
 /* Allocation-free burn.  No counterpart in the reference: it exists for
- * callers that must not allocate device memory when they burn -- code that
- * runs while a stream is being captured into a CUDA graph (cudaMalloc is not
- * allowed there), serving loops whose memory is budgeted up front and must
- * not grow or synchronise the device behind the caller's back, and plugin
- * hosts that own every allocation.  Same arguments and results as
+ * callers that must not allocate device memory when they burn -- serving
+ * loops whose device memory is budgeted up front and must not grow, or stall
+ * on cudaMalloc/cudaFree (which can synchronise the device), behind the
+ * caller's back, and plugin hosts (a database or GIS engine with its own pool
+ * allocator) that own every allocation.  Same arguments and results as
  * rz_rasterize, except:
  *   - no context: work goes to `stream` (a cudaStream_t, NULL = default);
  *   - the geometry arrays, per-geometry values, band_of_geom and `out` are

@@ -520,11 +520,11 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
 // ---------------------------------------------------------------------------
 // Allocation-free burn (rz_rasterize_noalloc).
 //
-// Some callers cannot allocate device memory at the moment they burn: code
-// running while a stream is being captured into a CUDA graph (cudaMalloc is
-// not allowed there), serving loops whose memory is budgeted up front and
-// must not grow or synchronise the device behind the caller's back, and
-// plugin hosts that own every allocation themselves.  This entry point runs
+// Some callers cannot allocate device memory at the moment they burn:
+// serving loops whose device memory is budgeted up front and must not grow,
+// or stall on cudaMalloc/cudaFree (which can synchronise the device) behind
+// the caller's back, and plugin hosts (a database or GIS engine with its own
+// pool allocator) that own every allocation themselves.  This entry point runs
 // the same kernels as rz_rasterize, but every scratch buffer is carved out of
 // the file-scope array below instead of the context's growable arena.  The
 // array is RZ_NOALLOC_SCRATCH_BYTES large and is held by every GPU that loads

@@ -2,9 +2,9 @@
 one, rz_rasterize, both called through the C ABI.
 
 rz_rasterize_noalloc is for callers that cannot allocate device memory at the
-moment they burn (work recorded while a stream is being captured into a CUDA
-graph, serving loops with a fixed memory budget, hosts that own every
-allocation): it takes device inputs and outputs and a stream, and takes all
+moment they burn (serving loops whose device memory is budgeted up front and
+must not grow or stall on cudaMalloc/cudaFree, plugin hosts that own every
+allocation through their own pool): it takes device inputs and outputs and a stream, and takes all
 of its scratch from one static device array of RZ_NOALLOC_SCRATCH_BYTES.
 Its results must be bit-identical to rz_rasterize's, also on the second of
 two calls in a row, whose scratch still holds the first call's contents.
