@@ -86,8 +86,8 @@ typedef struct {
  * context's stream, host time from a steady clock). */
 typedef struct {
   uint64_t edges;         /* polygon + line edges kept by the extract_* filters */
-  uint64_t crossings;     /* polygon scanline crossings evaluated (FP64) */
-  uint64_t spans;         /* span records after tile splitting */
+  uint64_t crossings;     /* polygon scanline crossings evaluated */
+  uint64_t spans;         /* coverage records: one per (part, row, 32-pixel word) covered */
   uint64_t pixel_writes;  /* pixels passed to the pixel function */
   uint64_t buckets;       /* (band, row, column-tile) buckets */
   uint64_t big_buckets;   /* buckets that took the block-level ordered path */

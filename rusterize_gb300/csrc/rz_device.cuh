@@ -14,13 +14,21 @@ namespace cg = cooperative_groups;
 
 // ---- tiling --------------------------------------------------------------
 // The output is cut into buckets of (band, row, column tile).  A tile is TW
-// pixels of one row; the fill kernels own one bucket at a time and write each
-// output pixel exactly once.
+// pixels (WPT 32-pixel words) of one row; the fill kernels own one bucket at
+// a time and write each output pixel exactly once.
 constexpr int TW_SHIFT = 9;
 constexpr int TW = 1 << TW_SHIFT;
-// span payload: x0 in bits 0-11, x1 in bits 12-23 (tile-local, x1 <= TW),
-// bit 31 = the part deduplicates its writes (PixelCache semantics).
-constexpr uint32_t X_MASK = 0xFFFu;
+constexpr int WPT = TW / 32;
+
+// Coverage records.  Span generation emits one record per (part, raster
+// row, 32-pixel word) that the part covers: the word id
+// ((band * nrows + row) * ntx * WPT + word of the row), the part and the
+// 32-bit mask of covered pixels.  After the scatter a record is
+// {part | word-in-tile << REC_W_SHIFT | DEDUP_BIT, mask}, grouped by bucket.
+constexpr uint32_t REC_W_SHIFT = 27;
+constexpr uint32_t REC_PART_MASK = (1u << REC_W_SHIFT) - 1u;  // parts are < 2^27
+// the part deduplicates its writes (PixelCache semantics): a pixel covered
+// by several records of the part is written once
 constexpr uint32_t DEDUP_BIT = 1u << 31;
 
 // Polygon scanline windows: per (part, row window) a parity bitmap of
@@ -28,22 +36,22 @@ constexpr uint32_t DEDUP_BIT = 1u << 31;
 // Narrow parts (bitmap row <= SMALL_BW words) take one warp per window with
 // a small bitmap; wider parts take one block per window.
 constexpr int BITMAP_WORDS = 8192;
-constexpr int WR_MAX = 64;
+constexpr int WR_MAX = 128;                 // rows per window
 constexpr int POLY_THREADS = 256;
-constexpr int POLY_QCAP = 1024;  // queued edges with crossings, per flush
-constexpr int POLY_SMEM = BITMAP_WORDS * 4 + POLY_QCAP * (3 * 8 + 2 * 4);
+constexpr int POLY_QENT = 32;               // bytes of one queued edge
+constexpr int POLY_WARP_QCAP = 64;          // queued edges per warp
+constexpr int POLY_SMEM = BITMAP_WORDS * 4 + (POLY_THREADS / 32) * POLY_WARP_QCAP * POLY_QENT;
 constexpr int SMALL_BW = 32;
 constexpr int SMALL_BITMAP_WORDS = 1024;
-constexpr int SMALL_QCAP = 128;
 constexpr int SMALL_WARPS = 4;  // warps (independent windows) per block
-constexpr int SMALL_WARP_SMEM = SMALL_BITMAP_WORDS * 4 + SMALL_QCAP * (3 * 8 + 2 * 4) + 3 * WR_MAX * 4 + 32;
+constexpr int SMALL_WARP_SMEM = POLY_WARP_QCAP * POLY_QENT + SMALL_BITMAP_WORDS * 4 + 3 * WR_MAX * 4 + 16;
 constexpr int SMALL_SMEM = SMALL_WARPS * SMALL_WARP_SMEM;
 
-// Fill: buckets with more than SMALL_MAX spans go to the block-level path,
-// which sorts up to BIG_CAP spans at a time in shared memory.
-constexpr int SMALL_MAX = 256;
-constexpr int BIG_CAP = 4096;
-constexpr int FILL_WARPS = 8;
+// Fill: buckets with at most FILL_WARP_MAX records are sorted and applied by
+// one warp; larger ones go to the per-word path, which takes at most
+// BIG_CAP records of one word at a time.
+constexpr int FILL_WARP_MAX = 64;
+constexpr int BIG_CAP = 1024;
 
 // Longest Bresenham walk one thread performs for a single segment.
 constexpr long long LINE_MAX_STEPS = 1ll << 26;
@@ -104,10 +112,11 @@ struct PartPlan {
 // wide parts and of narrow parts, line / point vertices, line / point parts.
 enum { PC_WINDOWS = 0, PC_WIN_SMALL, PC_LINE_V, PC_POINT_V, PC_LINE_P, PC_POINT_P, PC_N };
 
-struct SpanBuf {
-  unsigned* bucket;
-  unsigned* part;
-  unsigned* xs;
+// Coverage records before the scatter (structure of arrays).
+struct RecBuf {
+  unsigned* wid;   // word id
+  unsigned* part;  // part | DEDUP_BIT
+  unsigned* mask;  // covered pixels of the word
   unsigned long long cap;
 };
 
@@ -136,6 +145,9 @@ using rzb::floor_half_up;
 using rzb::floor_clamp;
 using rzb::half_int;
 using rzb::nan_bits;
+using rzb::CrossEdge;
+using rzb::cross_edge_setup;
+using rzb::cross_fast;
 
 // `(y - 0.5).ceil() as usize`, clamped to [0, nrows] (edges.rs:32-33).
 __device__ __forceinline__ int row_ceil(double py, int nrows) { return ceil_half_down(py, nrows); }
@@ -156,28 +168,28 @@ __device__ __forceinline__ long long as_isize(double v) {
   return (long long)v;
 }
 
-// Emit one span [xs, xe) of row `y` in `band` for `part`, cut at tile
-// boundaries.  Slots are taken with warp-aggregated atomics.
-__device__ __forceinline__ void emit_span(const SpanBuf& sb, unsigned* bucket_count, Ctrl* ctrl,
-                                          const Grid& g, unsigned band, int y, int xs, int xe,
-                                          unsigned part, unsigned flags) {
+// Emit the run [xs, xe) of row `y` in `band` for `part` as coverage
+// records, one per 32-pixel word.  Slots are taken with warp-aggregated
+// atomics.
+__device__ __forceinline__ void emit_run(const RecBuf& rb, unsigned* bucket_count, Ctrl* ctrl, const Grid& g,
+                                         unsigned band, int y, int xs, int xe, unsigned part_flags) {
   const unsigned long long rowid = (unsigned long long)band * (unsigned)g.nrows + (unsigned)y;
-  for (int t = xs >> TW_SHIFT; (t << TW_SHIFT) < xe; ++t) {
-    const int base = t << TW_SHIFT;
-    const unsigned a = (unsigned)(max(xs, base) - base);
-    const unsigned b = (unsigned)(min(xe, base + TW) - base);
-    const unsigned bucket = (unsigned)(rowid * g.ntx + (unsigned)t);
+  const unsigned row_wid = (unsigned)(rowid * g.ntx * WPT);
+  for (int wd = xs >> 5; (wd << 5) < xe; ++wd) {
+    const int lo = max(xs, wd << 5) - (wd << 5), hi = min(xe, (wd << 5) + 32) - (wd << 5);
+    const unsigned mask = (hi == 32 ? 0xFFFFFFFFu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+    const unsigned wid = row_wid + (unsigned)wd;
     cg::coalesced_group grp = cg::coalesced_threads();
     unsigned long long slot0 = 0;
     if (grp.thread_rank() == 0) slot0 = atomicAdd(&ctrl->span_count, (unsigned long long)grp.size());
     slot0 = grp.shfl(slot0, 0);
     const unsigned long long slot = slot0 + grp.thread_rank();
-    if (slot < sb.cap) {
-      sb.bucket[slot] = bucket;
-      sb.part[slot] = part;
-      sb.xs[slot] = a | (b << 12) | flags;
+    if (slot < rb.cap) {
+      rb.wid[slot] = wid;
+      rb.part[slot] = part_flags;
+      rb.mask[slot] = mask;
     }
-    atomicAdd(&bucket_count[bucket], 1u);
+    atomicAdd(&bucket_count[wid / WPT], 1u);
   }
 }
 

@@ -239,11 +239,11 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   const unsigned long long out_elems = nb * nrows * ncols;
   const unsigned ntx = (unsigned)((ncols + TW - 1) >> TW_SHIFT);
   const unsigned long long nbuckets = nb * nrows * ntx;
-  if (nbuckets >= 0xFFFFFFFFull)
-    return fail(err, errlen, RZ_VALUE_ERROR, "raster too large: more than 2^32 (band,row,tile) buckets");
+  if (nbuckets >= (1ull << 28))
+    return fail(err, errlen, RZ_VALUE_ERROR, "raster too large: more than 2^28 (band,row,tile) buckets");
   const unsigned long long G = g->n_geoms, P = g->n_parts, R = g->n_rings, V = g->n_vertices;
-  if (G >= 0xFFFFFFFFull || P >= 0xFFFFFFFFull)
-    return fail(err, errlen, RZ_VALUE_ERROR, "at most 2^32-1 geometries and parts are supported");
+  if (G >= 0xFFFFFFFFull || P >= (1ull << 27))
+    return fail(err, errlen, RZ_VALUE_ERROR, "at most 2^32-1 geometries and 2^27 parts are supported");
   if (!g->part_offsets || !g->part_kind || !g->ring_offsets || !g->vertex_offsets || (V && !g->xy))
     return fail(err, errlen, RZ_INVALID_ARGUMENT, "geometry table has null arrays");
   if (in_dev && (reinterpret_cast<uintptr_t>(g->xy) & 15))
@@ -400,12 +400,12 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     cap &= ~1ull;  // keeps the sorted {part, xs} array 8-byte aligned
     RZ_CUDA(ensure(ctx->spans, 20 * cap + 16));
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[7], s));
-    SpanBuf sb;
+    RecBuf sb;
     sb.cap = cap;
-    sb.bucket = static_cast<unsigned*>(ctx->spans.p);
-    sb.part = sb.bucket + cap;
-    sb.xs = sb.part + cap;
-    uint2* sorted = reinterpret_cast<uint2*>(sb.xs + cap);
+    sb.wid = static_cast<unsigned*>(ctx->spans.p);
+    sb.part = sb.wid + cap;
+    sb.mask = sb.part + cap;
+    uint2* sorted = reinterpret_cast<uint2*>(sb.mask + cap);
     k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
     RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
     launches += 1;
@@ -428,7 +428,7 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
     FillArgs fa;
     fa.offsets = boff;
-    fa.spans = sorted;
+    fa.recs = sorted;
     fa.nbuckets = nbuckets;
     fa.values = d_values;
     fa.scalar = scalar_bits;
@@ -445,7 +445,7 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     fa.ntx = ntx;
     fa.big = big;
     fa.ctrl = d_ctrl;
-    fa.span_cap = cap;
+    fa.rec_cap = cap;
     launches += fill(fa, (int)fn, dedup, sms, s);
     RZ_CUDA(cudaGetLastError());
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[5], s));
@@ -567,8 +567,8 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   const unsigned ntx = (unsigned)((ncols + TW - 1) >> TW_SHIFT);
   const unsigned long long nbuckets = nb * nrows * ntx;
   const unsigned long long G = g->n_geoms, P = g->n_parts, R = g->n_rings, V = g->n_vertices;
-  if (G >= 0xFFFFFFFFull || P >= 0xFFFFFFFFull || nbuckets >= 0xFFFFFFFFull)
-    return fail(err, errlen, RZ_VALUE_ERROR, "job too large for 32-bit part / bucket indices");
+  if (G >= 0xFFFFFFFFull || P >= (1ull << 27) || nbuckets >= (1ull << 28))
+    return fail(err, errlen, RZ_VALUE_ERROR, "job too large: at most 2^27 parts and 2^28 (band,row,tile) buckets");
   if (!g->part_offsets || !g->part_kind || !g->ring_offsets || !g->vertex_offsets || (V && !g->xy))
     return fail(err, errlen, RZ_INVALID_ARGUMENT, "geometry table has null arrays");
   if (reinterpret_cast<uintptr_t>(g->xy) & 15)
@@ -702,12 +702,12 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
     ++launches;
   }
   RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
-  SpanBuf sb;
+  RecBuf sb;
   sb.cap = cap;
-  sb.bucket = static_cast<unsigned*>(at(o_spans));
-  sb.part = sb.bucket + cap;
-  sb.xs = sb.part + cap;
-  uint2* sorted = reinterpret_cast<uint2*>(sb.xs + cap);
+  sb.wid = static_cast<unsigned*>(at(o_spans));
+  sb.part = sb.wid + cap;
+  sb.mask = sb.part + cap;
+  uint2* sorted = reinterpret_cast<uint2*>(sb.mask + cap);
   k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
   RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
   ++launches;
@@ -727,7 +727,7 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   ++launches;
   FillArgs fa;
   fa.offsets = boff;
-  fa.spans = sorted;
+  fa.recs = sorted;
   fa.nbuckets = nbuckets;
   fa.values = per_geom_values ? values : nullptr;
   fa.scalar = scalar_bits;
@@ -744,7 +744,7 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   fa.ntx = ntx;
   fa.big = big;
   fa.ctrl = d_ctrl;
-  fa.span_cap = cap;
+  fa.rec_cap = cap;
   launches += fill_for(dt)(fa, (int)fn, dedup, sms, s);
   RZ_CUDA(cudaGetLastError());
   Ctrl hc;  // the caller's stack, no pinned buffer

@@ -140,7 +140,8 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
             c_lo = floor(pxl - margin);
             c_hi = ceil(pxh + margin);
           }
-          const int col0 = c_lo <= 0.0 ? 0 : (c_lo >= g.ncols ? g.ncols : (int)c_lo);
+          // the bitmap starts on a 32-pixel word so that its words are raster words
+          const int col0 = (c_lo <= 0.0 ? 0 : (c_lo >= g.ncols ? g.ncols : (int)c_lo)) & ~31;
           const int colmax = c_hi <= 0.0 ? 0 : (c_hi >= g.ncols ? g.ncols : (int)c_hi);
           const int bw = (colmax - col0 + 1 + 31) >> 5;
           const bool narrow = bw <= SMALL_BW;
@@ -219,17 +220,17 @@ struct RunEmitter {
   unsigned long long npix = 0;
 };
 
-__device__ __forceinline__ void run_flush(RunEmitter& re, const SpanBuf& sb, unsigned* bucket_count,
+__device__ __forceinline__ void run_flush(RunEmitter& re, const RecBuf& sb, unsigned* bucket_count,
                                           Ctrl* ctrl, const Grid& g, unsigned band, unsigned part,
                                           unsigned flags) {
   if (re.y >= 0) {
     re.npix += (unsigned long long)(re.xb - re.xa);
-    emit_span(sb, bucket_count, ctrl, g, band, re.y, re.xa, re.xb, part, flags);
+    emit_run(sb, bucket_count, ctrl, g, band, re.y, re.xa, re.xb, part | flags);
   }
   re.y = -1;
 }
 
-__device__ __forceinline__ void run_add(RunEmitter& re, const SpanBuf& sb, unsigned* bucket_count, Ctrl* ctrl,
+__device__ __forceinline__ void run_add(RunEmitter& re, const RecBuf& sb, unsigned* bucket_count, Ctrl* ctrl,
                                         const Grid& g, unsigned band, unsigned part, unsigned flags, int y,
                                         int x) {
   if (re.y == y && x == re.xb) { re.xb = x + 1; return; }
@@ -246,7 +247,7 @@ __device__ __forceinline__ void run_add(RunEmitter& re, const SpanBuf& sb, unsig
 // part's last kept segment is written by k_line_endpix.
 __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
                              const unsigned long long* __restrict__ poff, const unsigned* __restrict__ line_parts,
-                             unsigned long long* last_kept, unsigned dedup_flag, SpanBuf sb,
+                             unsigned long long* last_kept, unsigned dedup_flag, RecBuf sb,
                              unsigned* bucket_count, Ctrl* ctrl) {
   if (ctrl->err) return;
   const unsigned long long nlist = poff[geo.n_parts * PC_N + PC_LINE_P];
@@ -302,7 +303,7 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
 // is written unless that segment's linestring is closed.
 __global__ void k_line_endpix(Geo geo, Grid g, const PartPlan* __restrict__ plan,
                               const unsigned long long* __restrict__ poff, const unsigned* __restrict__ line_parts,
-                              const unsigned long long* __restrict__ last_kept, unsigned dedup_flag, SpanBuf sb,
+                              const unsigned long long* __restrict__ last_kept, unsigned dedup_flag, RecBuf sb,
                               unsigned* bucket_count, Ctrl* ctrl) {
   if (ctrl->err) return;
   const unsigned long long nlist = poff[geo.n_parts * PC_N + PC_LINE_P];
@@ -321,7 +322,7 @@ __global__ void k_line_endpix(Geo geo, Grid g, const PartPlan* __restrict__ plan
     const long long ix = as_isize(floor(to_px(g, w1.x))), iy = as_isize(floor(to_py(g, w1.y)));
     if (ix >= 0 && ix < g.ncols && iy >= 0 && iy < g.nrows) {
       ++npix;
-      emit_span(sb, bucket_count, ctrl, g, plan[p].band, (int)iy, (int)ix, (int)ix + 1, p, dedup_flag);
+      emit_run(sb, bucket_count, ctrl, g, plan[p].band, (int)iy, (int)ix, (int)ix + 1, p | dedup_flag);
     }
   }
   if (npix) atomicAdd(&ctrl->pixel_writes, npix);
@@ -331,7 +332,7 @@ __global__ void k_line_endpix(Geo geo, Grid g, const PartPlan* __restrict__ plan
 // extract_point (edges.rs:79-88) + burn_point (burners.rs:250-258)
 __global__ void k_point_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
                               const unsigned long long* __restrict__ poff, const unsigned* __restrict__ point_parts,
-                              SpanBuf sb, unsigned* bucket_count, Ctrl* ctrl) {
+                              RecBuf sb, unsigned* bucket_count, Ctrl* ctrl) {
   if (ctrl->err) return;
   const unsigned long long nlist = poff[geo.n_parts * PC_N + PC_POINT_P];
   const unsigned long long total = poff[geo.n_parts * PC_N + PC_POINT_V];
@@ -349,7 +350,7 @@ __global__ void k_point_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan
     const double x = to_px(g, w.x), y = to_py(g, w.y);
     if (x >= 0.0 && x < (double)g.ncols && y >= 0.0 && y < (double)g.nrows) {
       ++npix;
-      emit_span(sb, bucket_count, ctrl, g, plan[p].band, (int)y, (int)x, (int)x + 1, p, 0u);
+      emit_run(sb, bucket_count, ctrl, g, plan[p].band, (int)y, (int)x, (int)x + 1, p);
     }
   }
   for (int o = 16; o > 0; o >>= 1) npix += __shfl_xor_sync(0xFFFFFFFFu, npix, o);
@@ -357,17 +358,33 @@ __global__ void k_point_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan
 }
 
 // ------------------------------------------------------------- scatter -----
-// Move each span into its bucket's range.  Order inside a bucket is
-// arbitrary here; the fill kernels restore part order.
-__global__ void k_scatter(SpanBuf sb, const unsigned* __restrict__ offsets, unsigned* counts, uint2* sorted,
+// Move each coverage record into its bucket's range as {part | word-in-tile
+// << REC_W_SHIFT | DEDUP_BIT, mask}.  Order inside a bucket is arbitrary
+// here; the fill kernels restore part order.  Records of one bucket that
+// sit in one warp (neighbouring words of a row) take their slots with one
+// atomic.
+__global__ void k_scatter(RecBuf sb, const unsigned* __restrict__ offsets, unsigned* counts, uint2* sorted,
                           Ctrl* ctrl) {
   if (ctrl->err || ctrl->span_count > sb.cap) return;
   const unsigned long long n = ctrl->span_count;
+  const int lane = threadIdx.x & 31;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-    const unsigned b = sb.bucket[i];
-    const unsigned pos = offsets[b] + atomicSub(&counts[b], 1u) - 1u;
-    sorted[pos] = make_uint2(sb.part[i], sb.xs[i]);
+  for (unsigned long long i0 = blockIdx.x * (unsigned long long)blockDim.x + (threadIdx.x & ~31u); i0 < n;
+       i0 += stride) {
+    const unsigned long long i = i0 + lane;
+    const bool valid = i < n;
+    const unsigned wid = valid ? sb.wid[i] : 0xFFFFFFFFu;
+    const unsigned b = valid ? wid / WPT : 0xFFFFFFFFu;
+    const unsigned same = __match_any_sync(0xFFFFFFFFu, b);
+    const int leader = __ffs(same) - 1;
+    unsigned top = 0;
+    if (valid && lane == leader) top = atomicSub(&counts[b], (unsigned)__popc(same));
+    top = __shfl_sync(0xFFFFFFFFu, top, leader);
+    if (valid) {
+      const unsigned rank = (unsigned)__popc(same & ((1u << lane) - 1u));
+      const unsigned pos = offsets[b] + top - 1u - rank;
+      sorted[pos] = make_uint2(sb.part[i] | ((wid % WPT) << REC_W_SHIFT), sb.mask[i]);
+    }
   }
 }
 

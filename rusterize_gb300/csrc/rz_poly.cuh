@@ -3,91 +3,110 @@
 // rust/src/geo/edges.rs:17-56 and extract_ring's filters, edges.rs:90-110).
 //
 // Work item: one (polygon part, row window).  Every crossing of an edge with
-// a scanline centre is evaluated in FP64 exactly as PolyEdge::intersect_at
-// and rounded to its pixel boundary r = clamp(floor(x + 0.5), 0, ncols).
-// That rounding is monotone, so pairing the x-sorted crossings two by two
-// (burners.rs:302-316) covers exactly the pixels whose count of boundaries
-// r <= x is odd: each crossing toggles bit r of a per-row parity bitmap and
-// spans are read back as consecutive pairs of set bits -- no sort is needed.
-// chunks_exact(2) drops the largest crossing of an odd row; such rows are
-// fixed up by toggling their maximum r once more.  Positive-NaN crossings
-// sort after every number (total_cmp) and only pair into empty spans, so they
-// are skipped; negative NaNs round to 0 and sort first.
+// a scanline centre is rounded to its pixel boundary
+// r = clamp(floor(x + 0.5), 0, ncols) with the value of
+// PolyEdge::intersect_at.  That rounding is monotone, so pairing the
+// x-sorted crossings two by two (burners.rs:302-316) covers exactly the
+// pixels whose count of boundaries r <= x is odd: each crossing toggles bit r
+// of a per-row parity bitmap and spans are read back as consecutive pairs of
+// set bits -- no sort is needed.  chunks_exact(2) drops the largest crossing
+// of an odd row; such rows are fixed up by toggling their maximum r once
+// more.  Positive-NaN crossings sort after every number (total_cmp) and only
+// pair into empty spans, so they are skipped; negative NaNs round to 0 and
+// sort first.
 //
-// FP64 is the narrow pipe on GB300, so the work is staged to keep every lane
-// busy when it issues FP64:
-//   1. one lane per vertex: y -> pixel and its first scanline (3 FP64 ops);
-//      edges that reach a scanline of the window are queued (ballot+popc)
-//   2. one lane per queued edge: horizontal filter, x -> pixel, slope
-//   3. crossings are dealt to lanes with a warp-shuffle prefix sum over the
-//      queued edges' row counts, so edges with very uneven row spans still
-//      keep all 32 lanes busy (4 FP64 ops per crossing)
-// Narrow parts run one window per warp (warp-level sync only, small bitmap);
-// wide parts run one window per block of POLY_THREADS.
+// FP64 is the narrow pipe on GB300.  The pixel coordinates of the vertices
+// are the reference's FP64 values, but the crossings are decided by the FP32
+// filter of rz_bits.h (cross_edge_setup's arithmetic / cross_fast), which
+// returns the FP64 boundary whenever it can prove it and otherwise hands the
+// crossing to the reference's FP64 sequence (cross_exact).
+//
+// Everything runs warp by warp, without block barriers inside a pass:
+//   1. vertex pass: one lane per vertex computes its pixel coordinates, first
+//      scanline and filter frame once; the lane owns the edge that ENDS at its
+//      vertex and gets the previous vertex by one register rotation (the
+//      chunk's first lane keeps the previous chunk's last vertex).  Edges with
+//      a scanline of the window are queued in shared memory.
+//   2. crossings: dealt to lanes in order over the queued edges' row counts,
+//      so edges with very uneven row spans keep all 32 lanes busy; each one
+//      toggles its bit in the window's bitmap (shared-memory atomics).
+//   3. extraction: the bitmap is read 32 words per round.  A pixel is
+//      covered when the number of boundaries at or left of it in its row is
+//      odd, so a word's coverage mask is the inclusive prefix XOR of its bits,
+//      inverted when the row's set bits before the word are odd in number
+//      (a row-segmented warp scan plus the previous round's carry).  Every
+//      non-zero mask becomes a coverage record, staged in shared memory and
+//      written out in coalesced runs with one slot reservation per flush.
+// Narrow parts run one window per warp; wide parts run one window per block
+// whose warps take contiguous vertex ranges and row ranges of the window.
 #pragma once
 
 #include "rz_device.cuh"
 
 namespace rzd {
 
-struct PolyQueue {
-  double* a;       // py0 -> y_top
-  double* b;       // py1 -> dxdy
-  double* c;       // x_top
-  unsigned* v;     // vertex index relative to the part | top flag (bit 31)
-  unsigned* rows;  // first row - r0 (bits 0-7) | row count (bits 8-15)
+// One queued edge in the crossing filter's frame (CrossEdge, rz_bits.h).
+struct __align__(16) QEnt {
+  int xi, yi;
+  float xf, g0, a, ee;
+  unsigned v;     // first vertex of the edge, relative to the part | top flag (bit 31)
+  unsigned rows;  // first row - r0 (bits 0-7) | row count (bits 8-15)
 };
+static_assert(sizeof(QEnt) == 32, "queue entry layout");
+
+constexpr int QCAP = POLY_WARP_QCAP;
+constexpr int STAGE_CAP = (QCAP * 32) / 12 / 8 * 8;  // staged records per warp (aliases the queue)
 
 struct PolyWin {
   int r0, r1, col0, nbits, bw;
 };
 
-template <int NT>  // cooperating threads: one warp (32) or the block
-__device__ __forceinline__ void scope_sync() {
-  if constexpr (NT == 32) __syncwarp(); else __syncthreads();
+// Per-warp shared-memory scratch: the edge queue, which doubles as the
+// record staging area between passes.
+struct WarpScratch {
+  QEnt* q;
+  unsigned* st_wid;
+  unsigned* st_part;
+  unsigned* st_mask;
+  __device__ __forceinline__ void init(void* base) {
+    q = reinterpret_cast<QEnt*>(base);
+    st_wid = reinterpret_cast<unsigned*>(base);
+    st_part = st_wid + STAGE_CAP;
+    st_mask = st_part + STAGE_CAP;
+  }
+};
+
+// The crossing of edge v (top end first when `top0`) with the centre of row
+// `row`, by the reference's FP64 sequence: PolyEdge::new's slope and
+// intersect_at (edges.rs:27-55), no FMA.  Used for the crossings the FP32
+// filter leaves undecided.  Returns the boundary, or -1 for a +NaN crossing.
+__device__ __noinline__ int cross_exact(const Geo& geo, const Grid& g, unsigned long long v, bool top0, int row) {
+  const double2 w0 = geo.xy[v], w1 = geo.xy[v + 1];
+  const double px0 = to_px(g, w0.x), py0 = to_py(g, w0.y), px1 = to_px(g, w1.x), py1 = to_py(g, w1.y);
+  const double xt = top0 ? px0 : px1, yt = top0 ? py0 : py1;
+  const double xb = top0 ? px1 : px0, yb = top0 ? py1 : py0;
+  const double dxdy = __ddiv_rn(__dsub_rn(xb, xt), __dsub_rn(yb, yt));
+  const double x = __dadd_rn(xt, __dmul_rn(__dsub_rn(half_int(row), yt), dxdy));
+  const unsigned long long xbits = f64_bits(x);
+  if (nan_bits(xbits)) return (xbits >> 63) ? 0 : -1;  // -NaN sorts first; +NaN pairs into an empty span
+  return floor_half_up(x, g.ncols);                    // floor(x + 0.5) clamped, burners.rs:310-311
 }
 
-template <int NT>
-__device__ __forceinline__ int scope_tid() {
-  if constexpr (NT == 32) return threadIdx.x & 31; else return threadIdx.x;
-}
-
-// stage 2 + 3 over the queued edges; MODE 0 toggles crossings, MODE 1
-// records the largest boundary of rows flagged odd.
-template <int MODE, int NT>
-__device__ __forceinline__ void poly_flush(const Geo& geo, const Grid& g, const PolyQueue& q, int nq,
+// Crossings of the nq queued edges; MODE 0 toggles them in the bitmap, MODE 1
+// records the largest boundary of rows flagged odd.  Lane j of a round takes
+// crossing m0 + j, whose edge is the last one starting at or before it.
+// Every queued edge has at least one row, so edge starts are distinct and one
+// OR-reduction of "start" bits plus a popcount finds it.
+template <int MODE>
+__device__ __forceinline__ void warp_cross(const Geo& geo, const Grid& g, const QEnt* q, int nq,
                                            unsigned long long vs, const PolyWin& w, unsigned* bm,
                                            const int* rowslot, int* oddmax, Ctrl* ctrl, unsigned long long part,
                                            unsigned long long& ncross) {
-  for (int i = scope_tid<NT>(); i < nq; i += NT) {
-    const double py0 = q.a[i], py1 = q.b[i];
-    const unsigned vv = q.v[i];
-    const bool top0 = vv >> 31;
-    const unsigned long long v = vs + (vv & 0x7FFFFFFFu);
-    // extract_ring's horizontal filter (edges.rs:100): |y0 - y1| >= EPSILON.
-    // Queued end points differ; two distinct doubles of magnitude >= 1 are
-    // at least 2^-52 apart, so only smaller ones need the subtraction.
-    if (!(abs_ge_one(py0) && abs_ge_one(py1))) {
-      const unsigned long long dbits = f64_bits(__dsub_rn(py0, py1)) & 0x7FFFFFFFFFFFFFFFull;
-      if (!(dbits >= 0x3CB0000000000000ull && dbits <= 0x7FF0000000000000ull)) {
-        q.rows[i] &= 0xFFu;  // no crossings
-        continue;
-      }
-    }
-    const double px0 = to_px(g, geo.xy[v].x), px1 = to_px(g, geo.xy[v + 1].x);
-    const double xt = top0 ? px0 : px1, yt = top0 ? py0 : py1;
-    const double xb = top0 ? px1 : px0, yb = top0 ? py1 : py0;
-    q.a[i] = yt;
-    q.b[i] = __ddiv_rn(__dsub_rn(xb, xt), __dsub_rn(yb, yt));  // edges.rs:36
-    q.c[i] = xt;
-  }
-  scope_sync<NT>();
   const int lane = threadIdx.x & 31;
-  const int first = NT == 32 ? 0 : (threadIdx.x >> 5) * 32;
-  for (int base = first; base < nq; base += NT) {
+  const unsigned lanemask_le = (2u << lane) - 1u;
+  for (int base = 0; base < nq; base += 32) {
     const int i = base + lane;
-    const unsigned rw = i < nq ? q.rows[i] : 0u;
-    const int n = (int)(rw >> 8);
+    const int n = i < nq ? (int)(q[i].rows >> 8) : 0;
     int incl = n;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -97,31 +116,29 @@ __device__ __forceinline__ void poly_flush(const Geo& geo, const Grid& g, const 
     const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     const int excl = incl - n;
     for (int m0 = 0; m0 < total; m0 += 32) {
+      const unsigned bit = (n > 0 && excl >= m0 && excl < m0 + 32) ? (1u << (excl - m0)) : 0u;
+      const unsigned starts = __reduce_or_sync(0xFFFFFFFFu, bit);
+      const int before = __popc(__ballot_sync(0xFFFFFFFFu, n > 0 && excl < m0));
+      const int s = before + __popc(starts & lanemask_le) - 1;
+      const int es = __shfl_sync(0xFFFFFFFFu, excl, s & 31);
       const int m = m0 + lane;
-      // largest source lane s with excl(s) <= m
-      int s = 0;
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int e = __shfl_sync(0xFFFFFFFFu, excl, s + step);
-        if (e <= m) s += step;
-      }
-      const int es = __shfl_sync(0xFFFFFFFFu, excl, s);
       if (m >= total) continue;
-      const int k = base + s;
-      const int rowrel = (int)(q.rows[k] & 0xFFu) + (m - es);
-      const double yt = q.a[k], dxdy = q.b[k], xt = q.c[k];
-      // PolyEdge::intersect_at (edges.rs:50-55), no FMA
-      const double cy = half_int(w.r0 + rowrel);
-      const double x = __dadd_rn(xt, __dmul_rn(__dsub_rn(cy, yt), dxdy));
-      const unsigned long long xb = f64_bits(x);
-      int r;
-      if (nan_bits(xb)) {
-        if (!(xb >> 63)) continue;  // +NaN: after every number, pairs into an empty span
-        r = 0;
-      } else {
-        r = floor_half_up(x, g.ncols);  // floor(x + 0.5) clamped, burners.rs:310-311
+      const QEnt qe = q[base + s];
+      const int row = w.r0 + (int)(qe.rows & 0xFFu) + (m - es);
+      CrossEdge ce;
+      ce.xi = qe.xi;
+      ce.yi = qe.yi;
+      ce.xf = qe.xf;
+      ce.g0 = qe.g0;
+      ce.a = qe.a;
+      ce.ee = qe.ee;
+      int r = cross_fast(ce, row, g.ncols);
+      if (r < 0) {
+        r = cross_exact(geo, g, vs + (qe.v & 0x7FFFFFFFu), qe.v >> 31, row);
+        if (r < 0) continue;
       }
       const int loc = r - w.col0;
+      const int rowrel = row - w.r0;
       if (loc < 0 || loc >= w.nbits) {
         set_error(ctrl, ERR_BITMAP, part);
         continue;
@@ -134,82 +151,251 @@ __device__ __forceinline__ void poly_flush(const Geo& geo, const Grid& g, const 
       }
     }
   }
-  scope_sync<NT>();
 }
 
-// Walk the part's edges once (stage 1), flushing the queue when it fills.
-template <int MODE, int NT, int QCAP>
-__device__ __forceinline__ void poly_pass(const Geo& geo, const Grid& g, unsigned long long rb, unsigned long long re,
-                                          const PolyWin& w, unsigned* bm, const PolyQueue& q, int* s_q,
-                                          const int* rowslot, int* oddmax, Ctrl* ctrl, unsigned long long part,
-                                          unsigned long long& ncross) {
-  const int lane = threadIdx.x & 31, tid = scope_tid<NT>();
-  const unsigned long long vs = geo.vertex_offsets[rb], ve = geo.vertex_offsets[re];
-  unsigned long long ring = rb;
-  for (unsigned long long base = vs; base < ve; base += NT) {
-    const unsigned long long v = base + tid;
+// Per-vertex values the vertex pass carries: pixel y (for the horizontal
+// filter), first scanline, and the filter frame of the vertex.
+struct VtxState {
+  double py;
+  int ys, xi, yi;
+  float xf, yf;
+  bool ok;
+};
+
+__device__ __forceinline__ VtxState vtx_state(const Grid& g, double2 w) {
+  VtxState s;
+  s.py = to_py(g, w.y);
+  s.ys = row_ceil(s.py, g.nrows);
+  const double px = to_px(g, w.x);
+  const bool okx = rzb::split_px(px, s.xi, s.xf);
+  const bool oky = rzb::split_px(s.py, s.yi, s.yf);
+  s.ok = okx && oky;
+  return s;
+}
+
+__device__ __forceinline__ VtxState rotate_prev(const VtxState& s, VtxState& carry, int lane) {
+  const int src = (lane + 31) & 31;
+  VtxState r;
+  r.py = __shfl_sync(0xFFFFFFFFu, s.py, src);
+  r.ys = __shfl_sync(0xFFFFFFFFu, s.ys, src);
+  r.xi = __shfl_sync(0xFFFFFFFFu, s.xi, src);
+  r.yi = __shfl_sync(0xFFFFFFFFu, s.yi, src);
+  r.xf = __shfl_sync(0xFFFFFFFFu, s.xf, src);
+  r.yf = __shfl_sync(0xFFFFFFFFu, s.yf, src);
+  r.ok = __shfl_sync(0xFFFFFFFFu, (int)s.ok, src) != 0;
+  if (lane == 0) {  // lane 0 receives this chunk's last vertex: the next chunk's predecessor
+    const VtxState prev = carry;
+    carry = r;
+    return prev;
+  }
+  return r;
+}
+
+// One warp walks vertices [vb, ve) of the part (indices relative to the
+// part's first vertex vs) and burns the crossings of the edges ending at
+// them into the window's bitmap.  Ring starts (no edge ends there) are the
+// part's first vertex and the ring ends of earlier rings; parts with at most
+// 32 rings keep those in registers.
+template <int MODE>
+__device__ __forceinline__ void warp_pass(const Geo& geo, const Grid& g, unsigned long long rb,
+                                          unsigned long long re, unsigned long long vs, unsigned vb, unsigned ve,
+                                          const PolyWin& w, unsigned* bm, QEnt* q, const int* rowslot, int* oddmax,
+                                          Ctrl* ctrl, unsigned long long part, unsigned long long& ncross) {
+  const int lane = threadIdx.x & 31;
+  if (vb >= ve) return;
+  const double2* xy = geo.xy + vs;
+  const unsigned nring = (unsigned)(re - rb);
+  const bool few = nring <= 32;
+  unsigned rend = 0xFFFFFFFFu;  // lane j: end (exclusive) of ring rb + j = start of the next ring
+  if (few && (unsigned)lane < nring) rend = (unsigned)(geo.vertex_offsets[rb + 1 + lane] - vs);
+  unsigned long long ring = rb;  // parts with many rings: ring of this lane's vertex
+  VtxState carry;
+  carry.py = 0.0;
+  carry.ys = carry.xi = carry.yi = 0;
+  carry.xf = carry.yf = 0.0f;
+  carry.ok = false;
+  if (vb > 0 && lane == 0) carry = vtx_state(g, xy[vb - 1]);
+  double2 wc = make_double2(0.0, 0.0);
+  if (vb + lane < ve) wc = xy[vb + lane];
+  int nq = 0;
+  for (unsigned base = vb; base < ve; base += 32) {
+    const unsigned v = base + lane;
     const bool has = v < ve;
-    double py0 = 0.0;
-    int ys0 = 0;
-    if (has) {
-      py0 = to_py(g, geo.xy[v].y);
-      ys0 = row_ceil(py0, g.nrows);
-    }
-    double py1 = __shfl_down_sync(0xFFFFFFFFu, py0, 1);
-    int ys1 = __shfl_down_sync(0xFFFFFFFFu, ys0, 1);
-    bool push = false;
-    unsigned rows = 0, vrel = 0;
-    if (has) {
-      if (geo.vertex_offsets[ring + 1] <= v) {
-        int steps = 0;
-        while (steps < 4 && geo.vertex_offsets[ring + 1] <= v) { ++ring; ++steps; }
-        if (geo.vertex_offsets[ring + 1] <= v) {
-          unsigned long long lo = ring, hi = re;  // vo[lo] <= v < vo[hi]
-          while (hi - lo > 1) {
-            const unsigned long long mid = (lo + hi) >> 1;
-            if (geo.vertex_offsets[mid] <= v) lo = mid; else hi = mid;
-          }
-          ring = lo;
+    double2 wn = make_double2(0.0, 0.0);
+    if (v + 32 < ve) wn = xy[v + 32];
+    bool start = v == 0;
+    if (few) {
+      for (unsigned j = 0; j < nring; ++j) start |= (v == __shfl_sync(0xFFFFFFFFu, rend, (int)j));
+    } else if (has) {
+      const unsigned long long va = vs + v;
+      if (geo.vertex_offsets[ring + 1] <= va) {
+        unsigned long long lo = ring, hi = re;  // vo[lo] <= va < vo[hi]
+        while (hi - lo > 1) {
+          const unsigned long long mid = (lo + hi) >> 1;
+          if (geo.vertex_offsets[mid] <= va) lo = mid; else hi = mid;
         }
+        ring = lo;
       }
-      if (v + 1 < geo.vertex_offsets[ring + 1]) {
-        if (lane == 31) {
-          py1 = to_py(g, geo.xy[v + 1].y);
-          ys1 = row_ceil(py1, g.nrows);
+      start = start || va == geo.vertex_offsets[ring];
+    }
+    const VtxState cur = vtx_state(g, wc);
+    const VtxState prv = rotate_prev(cur, carry, lane);
+    bool push = false;
+    QEnt e;
+    if (has && !start && prv.ys != cur.ys) {
+      // a scanline centre lies in [y_top, y_bot) iff the first scanlines of
+      // the end points differ; the raster-row filter (edges.rs:105) only
+      // removes edges without rows in [0, nrows).  The edge runs from the
+      // previous vertex (v - 1) to v.
+      const bool top0 = prv.ys < cur.ys;
+      const int a = max(top0 ? prv.ys : cur.ys, w.r0), b = min(top0 ? cur.ys : prv.ys, w.r1);
+      if (a < b) {
+        // horizontal filter |y0 - y1| >= EPSILON: two distinct doubles of
+        // magnitude >= 1 are at least 2^-52 apart, so only smaller end
+        // points need the subtraction
+        bool keep = true;
+        if (!(abs_ge_one(prv.py) && abs_ge_one(cur.py))) {
+          const unsigned long long dbits = f64_bits(__dsub_rn(prv.py, cur.py)) & 0x7FFFFFFFFFFFFFFFull;
+          keep = dbits >= 0x3CB0000000000000ull && dbits <= 0x7FF0000000000000ull;
         }
-        // a scanline centre lies in [y_top, y_bot) iff the first scanlines
-        // of the end points differ; the raster-row filter (edges.rs:105)
-        // only removes edges without rows in [0, nrows)
-        if (ys0 != ys1) {
-          const bool top0 = ys0 < ys1;
-          const int a = max(top0 ? ys0 : ys1, w.r0), b = min(top0 ? ys1 : ys0, w.r1);
-          if (a < b) {
-            push = true;
-            rows = (unsigned)(a - w.r0) | ((unsigned)(b - a) << 8);
-            vrel = (unsigned)(v - vs) | (top0 ? 0x80000000u : 0u);
-          }
+        if (keep) {
+          const VtxState& t = top0 ? prv : cur;
+          const VtxState& bt = top0 ? cur : prv;
+          CrossEdge ce;
+          rzb::cross_edge_frame(t.xi, t.xf, t.yi, t.yf, bt.xi, bt.xf, bt.yi, bt.yf, t.ok && bt.ok, ce);
+          e.xi = ce.xi;
+          e.yi = ce.yi;
+          e.xf = ce.xf;
+          e.g0 = ce.g0;
+          e.a = ce.a;
+          e.ee = ce.ee;
+          e.v = (v - 1) | (top0 ? 0x80000000u : 0u);
+          e.rows = (unsigned)(a - w.r0) | ((unsigned)(b - a) << 8);
+          push = true;
         }
       }
     }
     const unsigned mask = __ballot_sync(0xFFFFFFFFu, push);
-    if (mask) {
-      int pos0 = 0;
-      if (lane == 0) pos0 = atomicAdd(s_q, __popc(mask));
-      pos0 = __shfl_sync(0xFFFFFFFFu, pos0, 0);
-      if (push) {
-        const int pos = pos0 + __popc(mask & ((1u << lane) - 1u));
-        q.a[pos] = py0;
-        q.b[pos] = py1;
-        q.v[pos] = vrel;
-        q.rows[pos] = rows;
+    if (push) q[nq + __popc(mask & ((1u << lane) - 1u))] = e;
+    nq += __popc(mask);
+    if (nq > QCAP - 32 || base + 32 >= ve) {
+      __syncwarp();
+      if (nq > 0) warp_cross<MODE>(geo, g, q, nq, vs, w, bm, rowslot, oddmax, ctrl, part, ncross);
+      nq = 0;
+      __syncwarp();
+    }
+    wc = wn;
+  }
+}
+
+// ---- coverage extraction ----------------------------------------------------
+
+// Write the warp's staged records: one slot reservation, coalesced stores,
+// and one bucket-count update per run of equal buckets.
+__device__ __forceinline__ void stage_flush(WarpScratch& ws, int& st_n, const RecBuf& rb, unsigned* bucket_count,
+                                            Ctrl* ctrl) {
+  const int lane = threadIdx.x & 31;
+  if (st_n == 0) return;
+  __syncwarp();
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(&ctrl->span_count, (unsigned long long)st_n);
+  base = __shfl_sync(0xFFFFFFFFu, base, 0);
+  for (int j0 = 0; j0 < st_n; j0 += 32) {
+    const int j = j0 + lane;
+    const bool valid = j < st_n;
+    const unsigned wid = valid ? ws.st_wid[j] : 0xFFFFFFFFu;
+    if (valid) {
+      const unsigned long long slot = base + (unsigned)j;
+      if (slot < rb.cap) {
+        rb.wid[slot] = wid;
+        rb.part[slot] = ws.st_part[j];
+        rb.mask[slot] = ws.st_mask[j];
       }
     }
-    scope_sync<NT>();
-    const int nq = *s_q;
-    if (nq > QCAP - NT || base + NT >= ve) {
-      if (nq > 0) poly_flush<MODE, NT>(geo, g, q, nq, vs, w, bm, rowslot, oddmax, ctrl, part, ncross);
-      if (tid == 0) *s_q = 0;
-      scope_sync<NT>();
+    const unsigned bucket = valid ? wid / WPT : 0xFFFFFFFFu;
+    const unsigned same = __match_any_sync(0xFFFFFFFFu, bucket);
+    if (valid && (__ffs(same) - 1) == lane) atomicAdd(&bucket_count[bucket], (unsigned)__popc(same));
+  }
+  st_n = 0;
+  __syncwarp();
+}
+
+// Coverage records of rows [0, nr) of a bitmap of bw words per row (row i is
+// raster row r0 + i, bit b of word wd is column col0 + 32 wd + b; col0 is a
+// multiple of 32, so bitmap words are raster words).  Words are taken 32 per
+// round; rows are contiguous runs of lanes, so the parity of the set bits
+// before each word comes from a row-segmented XOR scan plus the carry of the
+// previous round.
+__device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw, int r0, int col0, unsigned band,
+                                             unsigned part, const Grid& g, WarpScratch& ws, int& st_n,
+                                             const RecBuf& rb, unsigned* bucket_count, Ctrl* ctrl,
+                                             unsigned long long& npix) {
+  const int lane = threadIdx.x & 31;
+  const int nw = nr * bw;
+  const float inv_bw = 1.0f / (float)bw;
+  const unsigned wpr = g.ntx * WPT;  // record words per raster row
+  const unsigned band_wid = band * (unsigned)g.nrows;
+  const unsigned w0 = (unsigned)col0 >> 5;
+  int c_row = -1;
+  unsigned c_par = 0;
+  for (int i0 = 0; i0 < nw; i0 += 32) {
+    const int i = i0 + lane;
+    const bool valid = i < nw;
+    // i / bw exactly: (i + 0.5) / bw is at least 0.5 / bw away from an integer
+    const int row = valid ? (int)__fmul_rn(__fadd_rn((float)i, 0.5f), inv_bw) : 0x7FFFFFFF;
+    const int wd = i - row * bw;
+    const unsigned bits = valid ? bm[i] : 0u;
+    unsigned par = (unsigned)__popc(bits) & 1u;
+    const unsigned own = par;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned tp = __shfl_up_sync(0xFFFFFFFFu, par, o);
+      const int tr = __shfl_up_sync(0xFFFFFFFFu, row, o);
+      if (lane >= o && tr == row) par ^= tp;
+    }
+    unsigned before = par ^ own;  // set bits of the row before this word (parity)
+    if (row == c_row) before ^= c_par;
+    {
+      const int lrow = __shfl_sync(0xFFFFFFFFu, row, 31);
+      unsigned lpar = __shfl_sync(0xFFFFFFFFu, par, 31);
+      if (lrow == c_row) lpar ^= c_par;
+      c_row = lrow;
+      c_par = lpar;
+    }
+    unsigned cov = bits;  // inclusive prefix XOR of the word's bits
+    cov ^= cov << 1;
+    cov ^= cov << 2;
+    cov ^= cov << 4;
+    cov ^= cov << 8;
+    cov ^= cov << 16;
+    if (before) cov = ~cov;
+    const bool emit = valid && cov != 0u;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, emit);
+    if (m == 0u) continue;
+    const int cnt = __popc(m);
+    if (cnt > STAGE_CAP - st_n) stage_flush(ws, st_n, rb, bucket_count, ctrl);
+    if (emit) {
+      const int k = st_n + __popc(m & ((1u << lane) - 1u));
+      ws.st_wid[k] = (band_wid + (unsigned)(r0 + row)) * wpr + w0 + (unsigned)wd;
+      ws.st_part[k] = part;
+      ws.st_mask[k] = cov;
+      npix += (unsigned long long)__popc(cov);
+    }
+    st_n += cnt;
+  }
+}
+
+// rows of the window with an odd number of crossings (one lane per row)
+__device__ __forceinline__ void warp_find_odd_rows(const unsigned* bm, int rb, int re, int bw, int* rowslot,
+                                                   int* oddrow, int* oddmax, int* s_nodd) {
+  for (int i = rb + (threadIdx.x & 31); i < re; i += 32) {
+    unsigned par = 0;
+    for (int wd = 0; wd < bw; ++wd) par ^= (unsigned)__popc(bm[i * bw + wd]);
+    if (par & 1u) {
+      const int slot = atomicAdd(s_nodd, 1);
+      rowslot[i] = slot;
+      oddrow[slot] = i;
+      oddmax[slot] = -1;
     }
   }
 }
@@ -235,280 +421,6 @@ __device__ __forceinline__ unsigned long long window_part(const unsigned long lo
   return lo;
 }
 
-// rows with an odd number of crossings; NT threads, rows dealt to warps
-template <int NT>
-__device__ __forceinline__ void find_odd_rows(const unsigned* bm, int nr, int bw, int* rowslot, int* oddrow,
-                                              int* oddmax, int* s_nodd) {
-  const int lane = threadIdx.x & 31;
-  const int warp = NT == 32 ? 0 : (threadIdx.x >> 5);
-  for (int i = warp; i < nr; i += NT / 32) {
-    unsigned par = 0;
-    for (int wd = lane; wd < bw; wd += 32) par ^= (unsigned)__popc(bm[i * bw + wd]) & 1u;
-    par = __reduce_xor_sync(0xFFFFFFFFu, par);
-    if (lane == 0 && par) {
-      const int slot = atomicAdd(s_nodd, 1);
-      rowslot[i] = slot;
-      oddrow[slot] = i;
-      oddmax[slot] = -1;
-    }
-  }
-}
-
-// Spans of one bitmap row = pairs of consecutive set bits.  One warp walks
-// the row 32 words at a time; every lane hands each span whose end bit lies
-// in its word to `f(xs, xe, lane_rank)`, where lane_rank numbers the pieces
-// (tile-cut parts) of the row in x order.  Returns the row's piece count.
-template <typename F>
-__device__ __forceinline__ unsigned row_spans(const unsigned* row, int bw, int col0, F&& f) {
-  const int lane = threadIdx.x & 31;
-  unsigned carry_cnt = 0, carry_pieces = 0;
-  int carry_last = -1;
-  for (int wb = 0; wb < bw; wb += 32) {
-    const int wd = wb + lane;
-    const unsigned bits0 = wd < bw ? row[wd] : 0u;
-    const int cnt = __popc(bits0);
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-      if (lane >= o) incl += t;
-    }
-    int mx = bits0 ? wd * 32 + 31 - __clz(bits0) : -1;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xFFFFFFFFu, mx, o);
-      if (lane >= o) mx = max(mx, t);
-    }
-    int prev0 = __shfl_up_sync(0xFFFFFFFFu, mx, 1);
-    if (lane == 0) prev0 = -1;
-    prev0 = max(prev0, carry_last);
-    const unsigned g0 = carry_cnt + (unsigned)(incl - cnt);
-    // pass a: this lane's piece count
-    unsigned bits = bits0, gidx = g0, mine = 0;
-    int prev = prev0;
-    while (bits) {
-      const int pos = wd * 32 + __ffs(bits) - 1;
-      bits &= bits - 1;
-      if (gidx & 1u) {
-        const int xs = col0 + prev, xe = col0 + pos;
-        mine += (unsigned)(((xe - 1) >> TW_SHIFT) - (xs >> TW_SHIFT) + 1);
-      }
-      prev = pos;
-      ++gidx;
-    }
-    unsigned pin = mine;
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned t = __shfl_up_sync(0xFFFFFFFFu, pin, o);
-      if (lane >= o) pin += t;
-    }
-    // pass b: hand the spans out with their rank
-    unsigned rank = carry_pieces + pin - mine;
-    bits = bits0;
-    gidx = g0;
-    prev = prev0;
-    while (bits) {
-      const int pos = wd * 32 + __ffs(bits) - 1;
-      bits &= bits - 1;
-      if (gidx & 1u) {
-        const int xs = col0 + prev, xe = col0 + pos;
-        f(xs, xe, rank);
-        rank += (unsigned)(((xe - 1) >> TW_SHIFT) - (xs >> TW_SHIFT) + 1);
-      }
-      prev = pos;
-      ++gidx;
-    }
-    carry_cnt += (unsigned)__shfl_sync(0xFFFFFFFFu, incl, 31);
-    carry_pieces += __shfl_sync(0xFFFFFFFFu, pin, 31);
-    carry_last = max(carry_last, __shfl_sync(0xFFFFFFFFu, mx, 31));
-  }
-  return carry_pieces;
-}
-
-// Emit the window's spans: count pieces per row, reserve all output slots
-// with ONE atomic, then write every piece at its rank (no per-span
-// round trip; bucket counts are fire-and-forget reductions).
-template <int NT>
-__device__ __forceinline__ void extract_spans(const unsigned* bm, const PolyWin& w, const PartPlan& pl,
-                                              unsigned long long p, const Grid& g, const SpanBuf& sb,
-                                              unsigned* bucket_count, Ctrl* ctrl, unsigned long long& npix,
-                                              unsigned* row_off, unsigned long long* s_base) {
-  const int lane = threadIdx.x & 31;
-  const int warp = NT == 32 ? 0 : (threadIdx.x >> 5);
-  const int nr = w.r1 - w.r0, bw = w.bw;
-  for (int i = warp; i < nr; i += NT / 32) {
-    const unsigned n = row_spans(bm + i * bw, bw, pl.col0, [](int, int, unsigned) {});
-    if (lane == 0) row_off[i] = n;
-  }
-  scope_sync<NT>();
-  if (warp == 0) {  // exclusive scan over <= 64 rows, reserve the window's slots
-    const unsigned a0 = lane < nr ? row_off[lane] : 0u, a1 = lane + 32 < nr ? row_off[lane + 32] : 0u;
-    unsigned i0 = a0, i1 = a1;
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned t0 = __shfl_up_sync(0xFFFFFFFFu, i0, o), t1 = __shfl_up_sync(0xFFFFFFFFu, i1, o);
-      if (lane >= o) { i0 += t0; i1 += t1; }
-    }
-    const unsigned tot0 = __shfl_sync(0xFFFFFFFFu, i0, 31);
-    const unsigned tot = tot0 + __shfl_sync(0xFFFFFFFFu, i1, 31);
-    __syncwarp();
-    if (lane < nr) row_off[lane] = i0 - a0;
-    if (lane + 32 < nr) row_off[lane + 32] = tot0 + i1 - a1;
-    if (lane == 0) *s_base = tot ? atomicAdd(&ctrl->span_count, (unsigned long long)tot) : 0ull;
-  }
-  scope_sync<NT>();
-  const unsigned long long base = *s_base;
-  const unsigned long long rowband = (unsigned long long)pl.band * (unsigned)g.nrows;
-  for (int i = warp; i < nr; i += NT / 32) {
-    const int y = w.r0 + i;
-    const unsigned long long rowid = rowband + (unsigned)y;
-    const unsigned long long rbase = base + row_off[i];
-    row_spans(bm + i * bw, bw, pl.col0, [&](int xs, int xe, unsigned rank) {
-      npix += (unsigned long long)(xe - xs);
-      for (int t = xs >> TW_SHIFT; (t << TW_SHIFT) < xe; ++t, ++rank) {
-        const int tb = t << TW_SHIFT;
-        const unsigned a = (unsigned)(max(xs, tb) - tb), b = (unsigned)(min(xe, tb + TW) - tb);
-        const unsigned bucket = (unsigned)(rowid * g.ntx + (unsigned)t);
-        const unsigned long long slot = rbase + rank;
-        if (slot < sb.cap) {
-          sb.bucket[slot] = bucket;
-          sb.part[slot] = (unsigned)p;
-          sb.xs[slot] = a | (b << 12);
-        }
-        atomicAdd(&bucket_count[bucket], 1u);
-      }
-    });
-  }
-}
-
-// Narrow parts (one warp per window): a row has at most SMALL_BW words, so
-// one LANE walks a whole row; the per-row piece offsets come from one warp
-// scan per 32 rows.
-__device__ __forceinline__ unsigned lane_row_pieces(const unsigned* row, int bw, int col0) {
-  unsigned par = 0, pieces = 0;
-  int start = 0;
-  for (int wd = 0; wd < bw; ++wd) {
-    unsigned bits = row[wd];
-    while (bits) {
-      const int pos = wd * 32 + __ffs(bits) - 1;
-      bits &= bits - 1;
-      if (par) {
-        const int xs = col0 + start, xe = col0 + pos;
-        pieces += (unsigned)(((xe - 1) >> TW_SHIFT) - (xs >> TW_SHIFT) + 1);
-      } else {
-        start = pos;
-      }
-      par ^= 1u;
-    }
-  }
-  return pieces;
-}
-
-__device__ __forceinline__ void find_odd_rows_lane(const unsigned* bm, int nr, int bw, int* rowslot, int* oddrow,
-                                                   int* oddmax, int* s_nodd) {
-  const int lane = threadIdx.x & 31;
-  for (int i = lane; i < nr; i += 32) {
-    unsigned par = 0;
-    for (int wd = 0; wd < bw; ++wd) par ^= (unsigned)__popc(bm[i * bw + wd]);
-    if (par & 1u) {
-      const int slot = atomicAdd(s_nodd, 1);
-      rowslot[i] = slot;
-      oddrow[slot] = i;
-      oddmax[slot] = -1;
-    }
-  }
-}
-
-__device__ __forceinline__ void extract_spans_lane(const unsigned* bm, const PolyWin& w, const PartPlan& pl,
-                                                   unsigned long long p, const Grid& g, const SpanBuf& sb,
-                                                   unsigned* bucket_count, Ctrl* ctrl, unsigned long long& npix) {
-  const int lane = threadIdx.x & 31;
-  const int nr = w.r1 - w.r0, bw = w.bw;
-  // pieces of rows lane and lane + 32, their exclusive offsets, one reservation
-  const unsigned c0 = lane < nr ? lane_row_pieces(bm + lane * bw, bw, pl.col0) : 0u;
-  const unsigned c1 = lane + 32 < nr ? lane_row_pieces(bm + (lane + 32) * bw, bw, pl.col0) : 0u;
-  unsigned i0 = c0, i1 = c1;
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned t0 = __shfl_up_sync(0xFFFFFFFFu, i0, o), t1 = __shfl_up_sync(0xFFFFFFFFu, i1, o);
-    if (lane >= o) { i0 += t0; i1 += t1; }
-  }
-  const unsigned tot0 = __shfl_sync(0xFFFFFFFFu, i0, 31);
-  const unsigned tot = tot0 + __shfl_sync(0xFFFFFFFFu, i1, 31);
-  unsigned long long base = 0;
-  if (lane == 0 && tot) base = atomicAdd(&ctrl->span_count, (unsigned long long)tot);
-  base = __shfl_sync(0xFFFFFFFFu, base, 0);
-  const unsigned long long rowband = (unsigned long long)pl.band * (unsigned)g.nrows;
-  for (int h = 0; h < 2; ++h) {
-    const int i = lane + 32 * h;
-    if (i >= nr) continue;
-    unsigned long long slot = base + (h == 0 ? i0 - c0 : tot0 + i1 - c1);
-    const unsigned long long rowid = rowband + (unsigned)(w.r0 + i);
-    const unsigned* row = bm + i * bw;
-    unsigned par = 0;
-    int start = 0;
-    for (int wd = 0; wd < bw; ++wd) {
-      unsigned bits = row[wd];
-      while (bits) {
-        const int pos = wd * 32 + __ffs(bits) - 1;
-        bits &= bits - 1;
-        if (par) {
-          const int xs = pl.col0 + start, xe = pl.col0 + pos;
-          npix += (unsigned long long)(xe - xs);
-          for (int t = xs >> TW_SHIFT; (t << TW_SHIFT) < xe; ++t, ++slot) {
-            const int tb = t << TW_SHIFT;
-            const unsigned a = (unsigned)(max(xs, tb) - tb), b = (unsigned)(min(xe, tb + TW) - tb);
-            const unsigned bucket = (unsigned)(rowid * g.ntx + (unsigned)t);
-            if (slot < sb.cap) {
-              sb.bucket[slot] = bucket;
-              sb.part[slot] = (unsigned)p;
-              sb.xs[slot] = a | (b << 12);
-            }
-            atomicAdd(&bucket_count[bucket], 1u);
-          }
-        } else {
-          start = pos;
-        }
-        par ^= 1u;
-      }
-    }
-  }
-}
-
-// one (part, window): zero the bitmap, toggle crossings, fix odd rows, emit
-template <int NT, int QCAP>
-__device__ __forceinline__ void poly_window(const Geo& geo, const Grid& g, const PartPlan& pl, unsigned long long p,
-                                            int k, unsigned* bm, const PolyQueue& q, int* s_q, int* rowslot,
-                                            int* oddmax, int* oddrow, int* s_nodd, unsigned long long* s_base,
-                                            const SpanBuf& sb, unsigned* bucket_count, Ctrl* ctrl,
-                                            unsigned long long& ncross, unsigned long long& npix) {
-  const int tid = scope_tid<NT>();
-  PolyWin win;
-  win.r0 = pl.row0 + k * pl.wr;
-  win.r1 = min(win.r0 + pl.wr, pl.row1);
-  win.col0 = pl.col0;
-  win.bw = pl.bw;
-  win.nbits = pl.bw * 32;
-  const int nr = win.r1 - win.r0, bw = pl.bw;
-  for (int i = tid; i < nr * bw; i += NT) bm[i] = 0u;
-  for (int i = tid; i < WR_MAX; i += NT) rowslot[i] = -1;
-  if (tid == 0) { *s_q = 0; *s_nodd = 0; }
-  scope_sync<NT>();
-  const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
-  poly_pass<0, NT, QCAP>(geo, g, rb, re, win, bm, q, s_q, rowslot, oddmax, ctrl, p, ncross);
-  if constexpr (NT == 32) find_odd_rows_lane(bm, nr, bw, rowslot, oddrow, oddmax, s_nodd);
-  else find_odd_rows<NT>(bm, nr, bw, rowslot, oddrow, oddmax, s_nodd);
-  scope_sync<NT>();
-  if (*s_nodd > 0) {
-    unsigned long long dummy = 0;
-    poly_pass<1, NT, QCAP>(geo, g, rb, re, win, bm, q, s_q, rowslot, oddmax, ctrl, p, dummy);
-    for (int t = tid; t < *s_nodd; t += NT) {
-      const int i = oddrow[t], loc = oddmax[t];
-      if (loc >= 0) bm[i * bw + (loc >> 5)] ^= 1u << (loc & 31);
-    }
-    scope_sync<NT>();
-  }
-  // oddrow is free again: it holds the per-row piece offsets
-  if constexpr (NT == 32) extract_spans_lane(bm, win, pl, p, g, sb, bucket_count, ctrl, npix);
-  else extract_spans<NT>(bm, win, pl, p, g, sb, bucket_count, ctrl, npix, reinterpret_cast<unsigned*>(oddrow), s_base);
-  scope_sync<NT>();
-}
-
 __device__ __forceinline__ void flush_counters(unsigned long long ncross, unsigned long long npix, Ctrl* ctrl) {
   for (int o = 16; o > 0; o >>= 1) {
     ncross += __shfl_xor_sync(0xFFFFFFFFu, ncross, o);
@@ -520,70 +432,36 @@ __device__ __forceinline__ void flush_counters(unsigned long long ncross, unsign
   }
 }
 
-// wide parts: one block per window
-__global__ void __launch_bounds__(POLY_THREADS) k_poly_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
-                                                              const unsigned long long* __restrict__ poff,
-                                                              SpanBuf sb, unsigned* bucket_count, Ctrl* ctrl) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  unsigned* bm = reinterpret_cast<unsigned*>(smem);
-  PolyQueue q;
-  q.a = reinterpret_cast<double*>(smem + BITMAP_WORDS * 4);
-  q.b = q.a + POLY_QCAP;
-  q.c = q.b + POLY_QCAP;
-  q.v = reinterpret_cast<unsigned*>(q.c + POLY_QCAP);
-  q.rows = q.v + POLY_QCAP;
-  __shared__ int rowslot[WR_MAX];
-  __shared__ int oddmax[WR_MAX];
-  __shared__ int oddrow[WR_MAX];
-  __shared__ int s_nodd, s_q;
-  __shared__ unsigned long long s_part, s_w, s_base;
-  if (ctrl->err) return;
-  const unsigned long long total = poff[geo.n_parts * PC_N + PC_WINDOWS];
-  unsigned long long ncross = 0, npix = 0;
-  while (true) {
-    if (threadIdx.x == 0) s_w = atomicAdd(&ctrl->work, 1ull);
-    __syncthreads();
-    const unsigned long long wi = s_w;
-    if (wi >= total) break;
-    if (threadIdx.x < 32) {
-      const unsigned long long p = window_part(poff, PC_WINDOWS, geo.n_parts, wi);
-      if (threadIdx.x == 0) s_part = p;
-    }
-    __syncthreads();
-    const unsigned long long p = s_part;
-    const PartPlan pl = plan[p];
-    const int k = (int)(wi - poff[p * PC_N + PC_WINDOWS]);
-    poly_window<POLY_THREADS, POLY_QCAP>(geo, g, pl, p, k, bm, q, &s_q, rowslot, oddmax, oddrow, &s_nodd, &s_base,
-                                         sb, bucket_count, ctrl, ncross, npix);
-  }
-  flush_counters(ncross, npix, ctrl);
+__device__ __forceinline__ PolyWin make_window(const PartPlan& pl, int k) {
+  PolyWin win;
+  win.r0 = pl.row0 + k * pl.wr;
+  win.r1 = min(win.r0 + pl.wr, pl.row1);
+  win.col0 = pl.col0;
+  win.bw = pl.bw;
+  win.nbits = pl.bw * 32;
+  return win;
 }
 
-// narrow parts: one warp per window, SMALL_WARPS independent warps per block
-__global__ void __launch_bounds__(SMALL_WARPS * 32, 4) k_poly_spans_narrow(Geo geo, Grid g,
+// ---- narrow parts: one window per warp ------------------------------------
+__global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo geo, Grid g,
                                                                         const PartPlan* __restrict__ plan,
                                                                         const unsigned long long* __restrict__ poff,
-                                                                        SpanBuf sb, unsigned* bucket_count,
+                                                                        RecBuf sb, unsigned* bucket_count,
                                                                         Ctrl* ctrl) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned char* base = smem + warp * SMALL_WARP_SMEM;
-  PolyQueue q;
-  q.a = reinterpret_cast<double*>(base);
-  q.b = q.a + SMALL_QCAP;
-  q.c = q.b + SMALL_QCAP;
-  q.v = reinterpret_cast<unsigned*>(q.c + SMALL_QCAP);
-  q.rows = q.v + SMALL_QCAP;
-  unsigned* bm = q.rows + SMALL_QCAP;
+  WarpScratch ws;
+  ws.init(base);
+  unsigned* bm = reinterpret_cast<unsigned*>(base + QCAP * sizeof(QEnt));
   int* rowslot = reinterpret_cast<int*>(bm + SMALL_BITMAP_WORDS);
   int* oddmax = rowslot + WR_MAX;
   int* oddrow = oddmax + WR_MAX;
-  unsigned long long* s_base = reinterpret_cast<unsigned long long*>(oddrow + WR_MAX);
-  int* s_q = reinterpret_cast<int*>(s_base + 1);
-  int* s_nodd = s_q + 1;
+  int* s_nodd = oddrow + WR_MAX;
   if (ctrl->err) return;
   const unsigned long long total = poff[geo.n_parts * PC_N + PC_WIN_SMALL];
   unsigned long long ncross = 0, npix = 0;
+  int st_n = 0;
   while (true) {
     unsigned long long wi = 0;
     if (lane == 0) wi = atomicAdd(&ctrl->work_small, 1ull);
@@ -592,8 +470,101 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 4) k_poly_spans_narrow(Geo g
     const unsigned long long p = window_part(poff, PC_WIN_SMALL, geo.n_parts, wi);
     const PartPlan pl = plan[p];
     const int k = (int)(wi - poff[p * PC_N + PC_WIN_SMALL]);
-    poly_window<32, SMALL_QCAP>(geo, g, pl, p, k, bm, q, s_q, rowslot, oddmax, oddrow, s_nodd, s_base, sb,
-                                bucket_count, ctrl, ncross, npix);
+    const PolyWin win = make_window(pl, k);
+    const int nr = win.r1 - win.r0, bw = pl.bw;
+    for (int i = lane; i < nr * bw; i += 32) bm[i] = 0u;
+    for (int i = lane; i < WR_MAX; i += 32) rowslot[i] = -1;
+    if (lane == 0) *s_nodd = 0;
+    const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
+    const unsigned long long vs = geo.vertex_offsets[rb];
+    const unsigned nv = (unsigned)(geo.vertex_offsets[re] - vs);
+    __syncwarp();
+    warp_pass<0>(geo, g, rb, re, vs, 0, nv, win, bm, ws.q, rowslot, oddmax, ctrl, p, ncross);
+    __syncwarp();
+    warp_find_odd_rows(bm, 0, nr, bw, rowslot, oddrow, oddmax, s_nodd);
+    __syncwarp();
+    const int nodd = *s_nodd;
+    if (nodd > 0) {
+      unsigned long long dummy = 0;
+      warp_pass<1>(geo, g, rb, re, vs, 0, nv, win, bm, ws.q, rowslot, oddmax, ctrl, p, dummy);
+      __syncwarp();
+      for (int t = lane; t < nodd; t += 32) {
+        const int i = oddrow[t], loc = oddmax[t];
+        if (loc >= 0) bm[i * bw + (loc >> 5)] ^= 1u << (loc & 31);
+      }
+      __syncwarp();
+    }
+    warp_extract(bm, nr, bw, win.r0, win.col0, pl.band, (unsigned)p, g, ws, st_n, sb, bucket_count, ctrl, npix);
+    stage_flush(ws, st_n, sb, bucket_count, ctrl);  // the stage aliases the queue of the next window
+  }
+  flush_counters(ncross, npix, ctrl);
+}
+
+// ---- wide parts: one window per block ---------------------------------------
+// Warp w walks vertices [w nv / W, (w + 1) nv / W) with its own queue and
+// extracts rows [w nr / W, (w + 1) nr / W); the bitmap is shared.
+__global__ void __launch_bounds__(POLY_THREADS) k_poly_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
+                                                              const unsigned long long* __restrict__ poff,
+                                                              RecBuf sb, unsigned* bucket_count, Ctrl* ctrl) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int W = POLY_THREADS / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned* bm = reinterpret_cast<unsigned*>(smem);
+  WarpScratch ws;
+  ws.init(smem + BITMAP_WORDS * 4 + warp * QCAP * sizeof(QEnt));
+  __shared__ int rowslot[WR_MAX];
+  __shared__ int oddmax[WR_MAX];
+  __shared__ int oddrow[WR_MAX];
+  __shared__ int s_nodd;
+  __shared__ unsigned long long s_part, s_w;
+  if (ctrl->err) return;
+  const unsigned long long total = poff[geo.n_parts * PC_N + PC_WINDOWS];
+  unsigned long long ncross = 0, npix = 0;
+  int st_n = 0;
+  while (true) {
+    if (threadIdx.x == 0) s_w = atomicAdd(&ctrl->work, 1ull);
+    __syncthreads();
+    const unsigned long long wi = s_w;
+    if (wi >= total) break;
+    if (warp == 0) {
+      const unsigned long long p = window_part(poff, PC_WINDOWS, geo.n_parts, wi);
+      if (lane == 0) s_part = p;
+    }
+    __syncthreads();
+    const unsigned long long p = s_part;
+    const PartPlan pl = plan[p];
+    const int k = (int)(wi - poff[p * PC_N + PC_WINDOWS]);
+    const PolyWin win = make_window(pl, k);
+    const int nr = win.r1 - win.r0, bw = pl.bw;
+    for (int i = threadIdx.x; i < nr * bw; i += POLY_THREADS) bm[i] = 0u;
+    for (int i = threadIdx.x; i < WR_MAX; i += POLY_THREADS) rowslot[i] = -1;
+    if (threadIdx.x == 0) s_nodd = 0;
+    const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
+    const unsigned long long vs = geo.vertex_offsets[rb];
+    const unsigned nv = (unsigned)(geo.vertex_offsets[re] - vs);
+    const unsigned vb = (unsigned)((unsigned long long)nv * warp / W);
+    const unsigned ve = (unsigned)((unsigned long long)nv * (warp + 1) / W);
+    __syncthreads();
+    warp_pass<0>(geo, g, rb, re, vs, vb, ve, win, bm, ws.q, rowslot, oddmax, ctrl, p, ncross);
+    __syncthreads();
+    const int rlo = nr * warp / W, rhi = nr * (warp + 1) / W;
+    warp_find_odd_rows(bm, rlo, rhi, bw, rowslot, oddrow, oddmax, &s_nodd);
+    __syncthreads();
+    const int nodd = s_nodd;
+    if (nodd > 0) {
+      unsigned long long dummy = 0;
+      warp_pass<1>(geo, g, rb, re, vs, vb, ve, win, bm, ws.q, rowslot, oddmax, ctrl, p, dummy);
+      __syncthreads();
+      for (int t = threadIdx.x; t < nodd; t += POLY_THREADS) {
+        const int i = oddrow[t], loc = oddmax[t];
+        if (loc >= 0) bm[i * bw + (loc >> 5)] ^= 1u << (loc & 31);
+      }
+      __syncthreads();
+    }
+    warp_extract(bm + rlo * bw, rhi - rlo, bw, win.r0 + rlo, win.col0, pl.band, (unsigned)p, g, ws, st_n, sb,
+                 bucket_count, ctrl, npix);
+    stage_flush(ws, st_n, sb, bucket_count, ctrl);
+    __syncthreads();
   }
   flush_counters(ncross, npix, ctrl);
 }
