@@ -15,10 +15,20 @@
 
 namespace rzb {
 
+// The bit pattern of v.  On the device it is taken by an opaque move, so
+// the compiler cannot fold the integer tests below back into FP64 compare
+// instructions (GB300's FP64 unit retires 2 lanes per clock per SM; the
+// integer pipe 64).
 RZ_HD uint64_t f64_bits(double v) {
+#if defined(__CUDA_ARCH__)
+  uint64_t b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(v));
+  return b;
+#else
   uint64_t b;
   memcpy(&b, &v, 8);
   return b;
+#endif
 }
 
 RZ_HD double bits_f64(uint64_t b) {

@@ -88,6 +88,17 @@ fill_fn fill_for(rz_dtype dt) {
   return nullptr;
 }
 
+// the scatter, instantiated for the value size of the output dtype
+void launch_scatter(size_t tsize, int sms, cudaStream_t s, const RecBuf& sb, const unsigned* boff, unsigned* bcount,
+                    uint2* sorted, const void* values, const unsigned* part_geom, void* rvals, Ctrl* ctrl) {
+  switch (tsize) {
+    case 1: k_scatter<1><<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, values, part_geom, rvals, ctrl); break;
+    case 2: k_scatter<2><<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, values, part_geom, rvals, ctrl); break;
+    case 4: k_scatter<4><<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, values, part_geom, rvals, ctrl); break;
+    default: k_scatter<8><<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, values, part_geom, rvals, ctrl); break;
+  }
+}
+
 unsigned grid_for(unsigned long long work, unsigned per_block, unsigned cap) {
   unsigned long long g = (work + per_block - 1) / per_block;
   if (g < 1) g = 1;
@@ -295,8 +306,8 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   if (!out_dev) RZ_CUDA(ensure(ctx->out, out_elems * tsize));
   unsigned long long cap = std::max<unsigned long long>(ctx->span_cap_hint, 2 * V + (1ull << 20));
   if (cap > 0xFFFFFFF0ull) cap = 0xFFFFFFF0ull;
-  RZ_CUDA(ensure(ctx->spans, 20 * cap + 16));
-  cap = std::min<unsigned long long>((ctx->spans.cap - 16) / 20, 0xFFFFFFF0ull) & ~1ull;
+  RZ_CUDA(ensure(ctx->spans, RECORD_BYTES * cap + 16));
+  cap = std::min<unsigned long long>((ctx->spans.cap - 16) / RECORD_BYTES, 0xFFFFFFF0ull) & ~1ull;
 
   char* mb = static_cast<char*>(ctx->main.p);
   auto at = [&](size_t o) { return static_cast<void*>(mb + o); };
@@ -398,7 +409,7 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   unsigned reruns = 0;
   while (true) {
     cap &= ~1ull;  // keeps the sorted {part, xs} array 8-byte aligned
-    RZ_CUDA(ensure(ctx->spans, 20 * cap + 16));
+    RZ_CUDA(ensure(ctx->spans, RECORD_BYTES * cap + 16));
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[7], s));
     RecBuf sb;
     sb.cap = cap;
@@ -406,6 +417,7 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     sb.part = sb.wid + cap;
     sb.mask = sb.part + cap;
     uint2* sorted = reinterpret_cast<uint2*>(sb.mask + cap);
+    void* rvals = sorted + cap;
     k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
     RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
     launches += 1;
@@ -423,16 +435,15 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     }
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[3], s));
     launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
-    k_scatter<<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, d_ctrl);
+    launch_scatter(tsize, sms, s, sb, boff, bcount, sorted, d_values, part_geom, rvals, d_ctrl);
     ++launches;
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
     FillArgs fa;
     fa.offsets = boff;
     fa.recs = sorted;
+    fa.rvals = d_values ? rvals : nullptr;
     fa.nbuckets = nbuckets;
-    fa.values = d_values;
     fa.scalar = scalar_bits;
-    fa.part_geom = part_geom;
     fa.out = d_out;
     fa.bg = bg_bits;
     {
@@ -600,12 +611,12 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   const size_t o_ctrl = L.take(sizeof(Ctrl));
   const size_t o_spans = L.take(0);
   const size_t min_spans = 1024;
-  if (o_spans + 20 * min_spans + 16 > RZ_NOALLOC_SCRATCH_BYTES)
+  if (o_spans + RECORD_BYTES * min_spans + 16 > RZ_NOALLOC_SCRATCH_BYTES)
     return fail(err, errlen, RZ_VALUE_ERROR,
                 "job needs %zu bytes of scratch before any span; the allocation-free entry point is limited to "
                 "%zu bytes (use rz_rasterize)",
-                o_spans + 20 * min_spans + 16, (size_t)RZ_NOALLOC_SCRATCH_BYTES);
-  unsigned long long cap = ((RZ_NOALLOC_SCRATCH_BYTES - o_spans - 16) / 20) & ~1ull;
+                o_spans + RECORD_BYTES * min_spans + 16, (size_t)RZ_NOALLOC_SCRATCH_BYTES);
+  unsigned long long cap = ((RZ_NOALLOC_SCRATCH_BYTES - o_spans - 16) / RECORD_BYTES) & ~1ull;
   if (cap > 0xFFFFFFF0ull) cap = 0xFFFFFFF0ull;
 
   int dev = 0;
@@ -708,6 +719,7 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   sb.part = sb.wid + cap;
   sb.mask = sb.part + cap;
   uint2* sorted = reinterpret_cast<uint2*>(sb.mask + cap);
+  void* rvals = sorted + cap;
   k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
   RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
   ++launches;
@@ -723,15 +735,15 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
     launches += 5;
   }
   launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
-  k_scatter<<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, d_ctrl);
+  const void* d_vals_na = per_geom_values ? values : nullptr;
+  launch_scatter(tsize, sms, s, sb, boff, bcount, sorted, d_vals_na, part_geom, rvals, d_ctrl);
   ++launches;
   FillArgs fa;
   fa.offsets = boff;
   fa.recs = sorted;
+  fa.rvals = d_vals_na ? rvals : nullptr;
   fa.nbuckets = nbuckets;
-  fa.values = per_geom_values ? values : nullptr;
   fa.scalar = scalar_bits;
-  fa.part_geom = part_geom;
   fa.out = out;
   fa.bg = bg_bits;
   {

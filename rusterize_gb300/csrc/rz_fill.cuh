@@ -17,10 +17,9 @@ namespace rzd {
 struct FillArgs {
   const unsigned* offsets;  // [nbuckets + 1]
   const uint2* recs;        // {part | word << REC_W_SHIFT | DEDUP_BIT, mask} grouped by bucket
+  const void* rvals;        // value of each record (T), or nullptr: every record burns `scalar`
   unsigned long long nbuckets;
-  const void* values;       // per-geometry values, or nullptr
-  unsigned long long scalar;  // raw bits of the single value when values == nullptr
-  const unsigned* part_geom;
+  unsigned long long scalar;  // raw bits of the single value when rvals == nullptr
   void* out;                // (bands, nrows, ncols)
   unsigned long long bg;    // raw bits of the background
   uint4 bg16;               // background replicated over 16 bytes
@@ -123,8 +122,8 @@ __device__ __forceinline__ T first_write(T v) {
 }
 
 template <typename T>
-__device__ __forceinline__ T value_of(const FillArgs& a, unsigned part) {
-  if (a.values) return static_cast<const T*>(a.values)[a.part_geom[part]];
+__device__ __forceinline__ T rec_value(const FillArgs& a, unsigned long long idx) {
+  if (a.rvals) return static_cast<const T*>(a.rvals)[idx];
   return from_bits<T>(a.scalar);
 }
 
@@ -218,18 +217,95 @@ __device__ __forceinline__ void apply_step(T& c, T v, bool on, T bg, const BgF64
 }
 
 // ---- warp fill -------------------------------------------------------------
-// One warp per bucket of at most FILL_WARP_MAX records.  Each record gets
-// its rank in (part, word) order by counting the smaller keys (ties broken
-// by position), is written to that slot with its value, and the records are
-// then applied in order: lane l owns pixel l of every word of the tile, so a
-// record is one broadcast load, a bit test and the pixel function.  Records
-// of one deduplicating part and word are adjacent in that order and write a
-// pixel once (PixelCache).
+// Buckets of at most FILL_WARP_MAX records, one warp each.  A warp takes 32
+// consecutive buckets (one coalesced load of their offsets) and loads the
+// next bucket's records and values while it works on the current one.
+//
+// Records of different words touch different pixels, so only the part
+// order within a word matters.  The records are sorted by (word, part) with
+// a bitonic network in registers (two records per lane) and then walked
+// once: lane l keeps pixel l of the current word in a register, applies
+// each record whose mask covers it, and stores the word when the walk moves
+// on (words without records are background).  A pixel-function step that
+// needs a float64 add issues it only when some lane of the warp needs it.
+// Records of one deduplicating part and word are adjacent in the order and
+// write a pixel once (PixelCache).
 constexpr int FILL_WARPS_PER_BLOCK = 8;
+constexpr int FILL_CHUNK = 32;
 
 template <typename T>
 constexpr int fill_warp_bytes() {
-  return TW * (int)sizeof(T) + FILL_WARP_MAX * (int)sizeof(SRec) + FILL_WARP_MAX * 4;
+  return FILL_WARP_MAX * (int)sizeof(SRec);
+}
+
+// the two records (positions lane and lane + 32) of a bucket held by a lane
+template <typename T>
+struct LanePair {
+  uint2 r0, r1;
+  T v0, v1;
+};
+
+template <typename T>
+__device__ __forceinline__ LanePair<T> load_pair(const FillArgs& a, unsigned o0, int n) {
+  const int lane = threadIdx.x & 31;
+  LanePair<T> p;
+  p.r0 = p.r1 = make_uint2(0u, 0u);
+  p.v0 = p.v1 = T(0);
+  if (n <= FILL_WARP_MAX) {
+    if (lane < n) {
+      p.r0 = a.recs[o0 + lane];
+      p.v0 = rec_value<T>(a, o0 + lane);
+    }
+    if (lane + 32 < n) {
+      p.r1 = a.recs[o0 + lane + 32];
+      p.v1 = rec_value<T>(a, o0 + lane + 32);
+    }
+  }
+  return p;
+}
+
+// One compare-exchange step of a bitonic network over elements held one per
+// lane (partner lane ^ j); `up` is the direction of this element's block.
+__device__ __forceinline__ void bitonic_step(unsigned& key, unsigned& idx, int j, bool up) {
+  const int lane = threadIdx.x & 31;
+  const unsigned pk = __shfl_xor_sync(0xFFFFFFFFu, key, j), pi = __shfl_xor_sync(0xFFFFFFFFu, idx, j);
+  const bool lower = (lane & j) == 0;
+  // keep the smaller element in the lower slot of an ascending block
+  const bool pless = pk < key || (pk == key && pi < idx);
+  if (lower == up ? pless : !pless) {
+    key = pk;
+    idx = pi;
+  }
+}
+
+// Sort (key, idx) pairs held at positions lane and lane + 32 ascending.
+__device__ __forceinline__ void warp_sort64(unsigned& k0, unsigned& i0, unsigned& k1, unsigned& i1, bool two) {
+  const int lane = threadIdx.x & 31;
+  // bitonic sort of each half (32 elements, one per lane); the second half
+  // descending when two halves are merged
+  for (int kk = 2; kk <= 32; kk <<= 1) {
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      const bool up0 = (lane & kk) == 0 || kk == 32;
+      bitonic_step(k0, i0, j, kk == 32 ? true : up0);
+      if (two) bitonic_step(k1, i1, j, kk == 32 ? false : ((lane & kk) == 0));
+    }
+  }
+  if (!two) return;
+  // merge: half 0 ascending, half 1 descending -> bitonic sequence of 64
+  {
+    const bool sw = k1 < k0 || (k1 == k0 && i1 < i0);
+    if (sw) {
+      const unsigned tk = k0, ti = i0;
+      k0 = k1;
+      i0 = i1;
+      k1 = tk;
+      i1 = ti;
+    }
+  }
+  for (int j = 16; j > 0; j >>= 1) {
+    bitonic_step(k0, i0, j, true);
+    bitonic_step(k1, i1, j, true);
+  }
 }
 
 template <typename T, int FN, bool DEDUP>
@@ -238,105 +314,136 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
   const Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned char* base = smem + warp * fill_warp_bytes<T>();
-  T* cur = reinterpret_cast<T*>(base);
-  SRec* srec = reinterpret_cast<SRec*>(base + TW * sizeof(T));
-  unsigned* keys = reinterpret_cast<unsigned*>(srec + FILL_WARP_MAX);
+  SRec* srec = reinterpret_cast<SRec*>(smem + warp * fill_warp_bytes<T>());
   const T bg = from_bits<T>(a.bg);
   const BgF64 bgc = bg_f64(a.bg);
   T* out = static_cast<T*>(a.out);
+  const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
   const unsigned long long nwarps = (unsigned long long)gridDim.x * FILL_WARPS_PER_BLOCK;
-  for (unsigned long long b = (unsigned long long)blockIdx.x * FILL_WARPS_PER_BLOCK + warp; b < a.nbuckets;
-       b += nwarps) {
-    const unsigned o0 = a.offsets[b];
-    const int n = (int)(a.offsets[b + 1] - o0);
-    const unsigned rowid = (unsigned)b / a.ntx;  // 32-bit: a 64-bit divide runs on the FP64 pipe
-    const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
-    const int len = min(TW, a.ncols - c0);
-    T* dst = out + (unsigned long long)rowid * (unsigned long long)a.ncols + c0;
-    if (n == 0) {
-      store_bg<T>(dst, len, a.bg16, bg, lane, 32);
-      continue;
-    }
-    if (n > FILL_WARP_MAX) {
-      if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
-      continue;
-    }
-    // this lane's records: positions lane and lane + 32
-    uint2 r0 = make_uint2(0u, 0u), r1 = make_uint2(0u, 0u);
-    unsigned k0 = 0xFFFFFFFFu, k1 = 0xFFFFFFFFu;
-    if (lane < n) { r0 = a.recs[o0 + lane]; k0 = rec_key(r0.x); }
-    if (lane + 32 < n) { r1 = a.recs[o0 + lane + 32]; k1 = rec_key(r1.x); }
-    T v0 = T(0), v1 = T(0);
-    if (lane < n) v0 = value_of<T>(a, r0.x & REC_PART_MASK);
-    if (lane + 32 < n) v1 = value_of<T>(a, r1.x & REC_PART_MASK);
-    if (lane < n) keys[lane] = k0;
-    if (lane + 32 < n) keys[lane + 32] = k1;
-    // background tile
-    {
-      uint4* c4 = reinterpret_cast<uint4*>(cur);
-      for (int i = lane; i < (int)(TW * sizeof(T) / 16); i += 32) c4[i] = a.bg16;
-    }
-    __syncwarp();
-    // rank = smaller keys + equal keys at smaller positions
-    int rk0 = 0, rk1 = 0;
-    for (int j = 0; j < n; ++j) {
-      const unsigned kj = keys[j];
-      rk0 += (kj < k0) || (kj == k0 && j < lane);
-      rk1 += (kj < k1) || (kj == k1 && j < lane + 32);
-    }
-    if (lane < n) {
-      SRec e;
-      e.key = k0 | (r0.x & DEDUP_BIT);
-      e.mask = r0.y;
-      e.vbits = to_bits<T>(v0);
-      srec[rk0] = e;
-    }
-    if (lane + 32 < n) {
-      SRec e;
-      e.key = k1 | (r1.x & DEDUP_BIT);
-      e.mask = r1.y;
-      e.vbits = to_bits<T>(v1);
-      srec[rk1] = e;
-    }
-    __syncwarp();
-    unsigned prev_key = 0xFFFFFFFFu, seen = 0u;
-    for (int j = 0; j < n; ++j) {
-      const SRec e = srec[j];
-      const unsigned key = e.key & ~DEDUP_BIT;
-      unsigned mask = e.mask;
-      if (DEDUP && (e.key & DEDUP_BIT)) {
-        if (key != prev_key) seen = 0u;
-        mask &= ~seen;
-        seen |= e.mask;
+  for (unsigned long long ch = (unsigned long long)blockIdx.x * FILL_WARPS_PER_BLOCK + warp; ch < nchunks;
+       ch += nwarps) {
+    const unsigned long long b0 = ch * FILL_CHUNK;
+    const int nb = (int)min((unsigned long long)FILL_CHUNK, a.nbuckets - b0);
+    const unsigned off = a.offsets[b0 + (lane < nb ? lane : nb)];
+    const unsigned off_end = a.offsets[b0 + nb];
+    unsigned o_next = __shfl_sync(0xFFFFFFFFu, off, 0);
+    int n_next = (int)((nb > 1 ? __shfl_sync(0xFFFFFFFFu, off, 1) : off_end) - o_next);
+    LanePair<T> nxt = load_pair<T>(a, o_next, n_next);
+    for (int k = 0; k < nb; ++k) {
+      const unsigned long long b = b0 + k;
+      const int n = n_next;
+      const LanePair<T> pr = nxt;
+      if (k + 1 < nb) {  // prefetch the next bucket
+        o_next = __shfl_sync(0xFFFFFFFFu, off, k + 1);
+        n_next = (int)((k + 2 < nb ? __shfl_sync(0xFFFFFFFFu, off, (k + 2) & 31) : off_end) - o_next);
+        nxt = load_pair<T>(a, o_next, n_next);
       }
-      prev_key = key;
-      const int w = (int)(key & 15u);
-      const bool on = (mask >> lane) & 1u;
-      T c = cur[w * 32 + lane];
-      apply_step<T, FN>(c, from_bits<T>(e.vbits), on, bg, bgc);
-      if (on) cur[w * 32 + lane] = c;
+      const unsigned rowid = (unsigned)b / a.ntx;  // 32-bit: a 64-bit divide runs on the FP64 pipe
+      const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
+      const int len = min(TW, a.ncols - c0);
+      T* dst = out + (unsigned long long)rowid * (unsigned long long)a.ncols + c0;
+      if (n == 0) {
+        store_bg<T>(dst, len, a.bg16, bg, lane, 32);
+        continue;
+      }
+      if (n > FILL_WARP_MAX) {
+        if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
+        continue;
+      }
+      // (word, part) keys; invalid positions sort last
+      unsigned k0 = lane < n ? pr.r0.x & ~DEDUP_BIT : 0xFFFFFFFFu, i0 = (unsigned)lane;
+      unsigned k1 = lane + 32 < n ? pr.r1.x & ~DEDUP_BIT : 0xFFFFFFFFu, i1 = (unsigned)lane + 32u;
+      const bool two = n > 32;
+      {
+        const unsigned nk0 = __shfl_down_sync(0xFFFFFFFFu, k0, 1), nk1 = __shfl_down_sync(0xFFFFFFFFu, k1, 1);
+        const unsigned k1_first = __shfl_sync(0xFFFFFFFFu, k1, 0);
+        const bool ord = k0 <= (lane == 31 ? k1_first : nk0) && (lane == 31 || k1 <= nk1);
+        if (!__all_sync(0xFFFFFFFFu, ord)) warp_sort64(k0, i0, k1, i1, two);
+      }
+      // sorted position p (lane p, then lane p - 32) holds original record i:
+      // fetch it from the lane that loaded it and store it at p
+      {
+        const int s0 = (int)(i0 & 31u), s1 = (int)(i1 & 31u);
+        const unsigned ax = __shfl_sync(0xFFFFFFFFu, pr.r0.x, s0), am = __shfl_sync(0xFFFFFFFFu, pr.r0.y, s0);
+        const T av = shfl_val<T>(pr.v0, s0);
+        SRec e;
+        if (two) {
+          const unsigned bx = __shfl_sync(0xFFFFFFFFu, pr.r1.x, s0), bm = __shfl_sync(0xFFFFFFFFu, pr.r1.y, s0);
+          const T bv = shfl_val<T>(pr.v1, s0);
+          const bool hi0 = i0 >= 32u;
+          e.key = hi0 ? bx : ax;
+          e.mask = hi0 ? bm : am;
+          e.vbits = to_bits<T>(hi0 ? bv : av);
+          if (lane < n) srec[lane] = e;
+          const unsigned cx = __shfl_sync(0xFFFFFFFFu, pr.r0.x, s1), cm = __shfl_sync(0xFFFFFFFFu, pr.r0.y, s1);
+          const T cv = shfl_val<T>(pr.v0, s1);
+          const unsigned dx = __shfl_sync(0xFFFFFFFFu, pr.r1.x, s1), dm = __shfl_sync(0xFFFFFFFFu, pr.r1.y, s1);
+          const T dv = shfl_val<T>(pr.v1, s1);
+          const bool hi1 = i1 >= 32u;
+          e.key = hi1 ? dx : cx;
+          e.mask = hi1 ? dm : cm;
+          e.vbits = to_bits<T>(hi1 ? dv : cv);
+          if (lane + 32 < n) srec[lane + 32] = e;
+        } else {
+          e.key = ax;
+          e.mask = am;
+          e.vbits = to_bits<T>(av);
+          if (lane < n) srec[lane] = e;
+        }
+      }
+      __syncwarp();
+      // walk the records once; lane l folds pixel l of the current word
+      int cw = -1;
+      T c = bg;
+      unsigned prev_key = 0xFFFFFFFFu, seen = 0u;
+      for (int p = 0; p < n; ++p) {
+        const SRec e = srec[p];
+        const int w = (int)((e.key >> REC_W_SHIFT) & 15u);
+        if (w != cw) {
+          if (cw >= 0 && cw * 32 + lane < len) dst[cw * 32 + lane] = c;
+          for (int ww = cw + 1; ww < w; ++ww)
+            if (ww * 32 + lane < len) dst[ww * 32 + lane] = bg;
+          cw = w;
+          c = bg;
+          prev_key = 0xFFFFFFFFu;
+        }
+        unsigned mask = e.mask;
+        if (DEDUP && (e.key & DEDUP_BIT)) {
+          const unsigned key = e.key & ~DEDUP_BIT;
+          if (key != prev_key) seen = 0u;
+          mask &= ~seen;
+          seen |= e.mask;
+          prev_key = key;
+        }
+        apply_step<T, FN>(c, from_bits<T>(e.vbits), (mask >> lane) & 1u, bg, bgc);
+      }
+      if (cw * 32 + lane < len) dst[cw * 32 + lane] = c;
+      for (int ww = cw + 1; ww < WPT; ++ww)
+        if (ww * 32 + lane < len) dst[ww * 32 + lane] = bg;
+      __syncwarp();
     }
-    __syncwarp();
-    store_tile<T>(dst, cur, len, lane, 32);
-    __syncwarp();
   }
 }
 
 // ---- deep buckets: one warp per (bucket, word) --------------------------
 // The word's records are taken in part order, at most BIG_CAP at a time: a
 // histogram over the pending part ids picks the largest prefix range that
-// fits, the range is gathered, sorted (bitonic, shared memory) and applied;
-// lane l keeps pixel l of the word in a register throughout.  A single part
-// with more than BIG_CAP records in the word is applied in chunks (its
-// records share one value and their order does not change the result).
+// fits, the range is gathered, sorted (bitonic, shared memory) and folded:
+// lane l keeps pixel l of the word in a register and walks the sorted
+// records to the next one covering its pixel, so every step applies one
+// record per lane.  A single part with more than BIG_CAP records in the word
+// is applied in chunks (its records share one value and their order does
+// not change the result).
 constexpr int BIG_WARPS = 4;
 constexpr int BIG_HIST = 256;
 
-constexpr int big_warp_bytes() { return BIG_CAP * 8 + BIG_HIST * 4; }
+template <typename T>
+constexpr int big_warp_bytes() { return BIG_CAP * 8 + BIG_CAP * (int)sizeof(T) + BIG_HIST * 4; }
 
-__device__ __forceinline__ void warp_sort_keys(unsigned long long* k, int n) {
-  // ascending bitonic sort of k[0..np) with np = next power of two >= n (padded with ~0)
+// ascending bitonic sort of k[0..np) with np = next power of two >= n
+// (padded with ~0), carrying v along
+template <typename T>
+__device__ __forceinline__ void warp_sort_keys(unsigned long long* k, T* v, int n) {
   int np = 1;
   while (np < n) np <<= 1;
   const int lane = threadIdx.x & 31;
@@ -349,11 +456,49 @@ __device__ __forceinline__ void warp_sort_keys(unsigned long long* k, int n) {
         if (ixj > i) {
           const unsigned long long x = k[i], y = k[ixj];
           const bool up = (i & kk) == 0;
-          if ((x > y) == up) { k[i] = y; k[ixj] = x; }
+          if ((x > y) == up) {
+            k[i] = y;
+            k[ixj] = x;
+            const T t = v[i];
+            v[i] = v[ixj];
+            v[ixj] = t;
+          }
         }
       }
       __syncwarp();
     }
+  }
+}
+
+// Fold keys[0..m) (part << 33 | dedup << 32 | mask, part order) into this
+// lane's pixel: each step every lane advances to the next record covering
+// its pixel (skipping repeats of a deduplicating part) and applies it.
+template <typename T, int FN, bool DEDUP>
+__device__ __forceinline__ void fold_sorted(const unsigned long long* keys, const T* vals, int m, T& c,
+                                            unsigned& last_part, T bg, const BgF64& bgc) {
+  const unsigned bit = 1u << (threadIdx.x & 31);
+  int j = 0;
+  bool active = true;
+  while (__any_sync(0xFFFFFFFFu, active)) {
+    T v = T(0);
+    bool on = false;
+    if (active) {
+      while (j < m) {
+        const unsigned long long kj = keys[j];
+        const unsigned part = (unsigned)(kj >> 33);
+        if (((unsigned)kj & bit) && !(DEDUP && ((kj >> 32) & 1u) && part == last_part)) break;
+        ++j;
+      }
+      if (j < m) {
+        on = true;
+        v = vals[j];
+        last_part = (unsigned)(keys[j] >> 33);
+        ++j;
+      } else {
+        active = false;
+      }
+    }
+    apply_step<T, FN>(c, v, on, bg, bgc);
   }
 }
 
@@ -363,8 +508,10 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
   const Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem + warp * big_warp_bytes());
-  unsigned* hist = reinterpret_cast<unsigned*>(keys + BIG_CAP);
+  unsigned char* wbase = smem + warp * big_warp_bytes<T>();
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(wbase);
+  T* vals = reinterpret_cast<T*>(wbase + BIG_CAP * 8);
+  unsigned* hist = reinterpret_cast<unsigned*>(wbase + BIG_CAP * 8 + BIG_CAP * sizeof(T));
   const T bg = from_bits<T>(a.bg);
   const BgF64 bgc = bg_f64(a.bg);
   T* out = static_cast<T*>(a.out);
@@ -379,8 +526,8 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
     const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
     const int x = c0 + (int)wsel * 32 + lane;
     T c = bg;
+    unsigned last_part = 0xFFFFFFFFu;
     unsigned lo_part = 0;  // parts < lo_part are done
-    unsigned prev_key = 0xFFFFFFFFu, seen = 0u;
     while (true) {
       unsigned cnt = 0, pmin = 0xFFFFFFFFu, pmax = 0;
       for (int i = lane; i < n; i += 32) {
@@ -396,7 +543,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
       if (cnt == 0) break;
       pmin = __reduce_min_sync(0xFFFFFFFFu, pmin);
       pmax = __reduce_max_sync(0xFFFFFFFFu, pmax);
-      unsigned hi = pmax + 1;  // parts [pmin, hi) this round
+      unsigned hi = pmax + 1;  // parts [lo_part, hi) this round
       bool single = false;
       if (cnt > (unsigned)BIG_CAP) {
         unsigned span_lo = pmin, span_hi = pmax;  // inclusive
@@ -436,7 +583,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
           span_hi = span_lo + (1u << shift) - 1u;  // zoom into the first bin
         }
       }
-      // gather [lo_part, hi) of this word, in chunks of BIG_CAP when single
+      // gather [lo_part, hi) of this word (chunks of BIG_CAP for a single part)
       int m = 0;
       for (int i0 = 0; i0 < n; i0 += 32) {
         const int i = i0 + lane;
@@ -451,49 +598,22 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
         if (take) {
           const int pos = m + __popc(mk & ((1u << lane) - 1u));
           // part (order), then the DEDUP flag, then the mask
-          keys[pos] = ((unsigned long long)(r.x & REC_PART_MASK) << 33) |
-                      ((unsigned long long)(r.x >> 31) << 32) | r.y;
+          keys[pos] = ((unsigned long long)(r.x & REC_PART_MASK) << 33) | ((unsigned long long)(r.x >> 31) << 32) |
+                      r.y;
+          vals[pos] = rec_value<T>(a, o0 + i);
         }
         m += __popc(mk);
-        if (single && m > BIG_CAP - 32) {  // flush a chunk of the single part
+        if (single && m > BIG_CAP - 32) {  // fold a chunk of the single part
           __syncwarp();
-          const T v = value_of<T>(a, hi - 1);
-          for (int j = 0; j < m; ++j) {
-            const unsigned long long kj = keys[j];
-            unsigned mask = (unsigned)kj;
-            const unsigned part = (unsigned)(kj >> 33);
-            if (DEDUP && ((kj >> 32) & 1u)) {
-              if (part != prev_key) seen = 0u;
-              mask &= ~seen;
-              seen |= (unsigned)kj;
-            }
-            prev_key = part;
-            apply_step<T, FN>(c, v, (mask >> lane) & 1u, bg, bgc);
-          }
+          fold_sorted<T, FN, DEDUP>(keys, vals, m, c, last_part, bg, bgc);
           m = 0;
           __syncwarp();
         }
       }
       __syncwarp();
-      if (!single) warp_sort_keys(keys, m);
-      for (int j0 = 0; j0 < m; j0 += 32) {  // values of this chunk, 32 at a time
-        T vj = T(0);
-        if (j0 + lane < m) vj = value_of<T>(a, (unsigned)(keys[j0 + lane] >> 33));
-        const int jn = min(32, m - j0);
-        for (int jj = 0; jj < jn; ++jj) {
-          const unsigned long long kj = keys[j0 + jj];
-          const T v = shfl_val<T>(vj, jj);
-          unsigned mask = (unsigned)kj;
-          const unsigned part = (unsigned)(kj >> 33);
-          if (DEDUP && ((kj >> 32) & 1u)) {
-            if (part != prev_key) seen = 0u;
-            mask &= ~seen;
-            seen |= (unsigned)kj;
-          }
-          prev_key = part;
-          apply_step<T, FN>(c, v, (mask >> lane) & 1u, bg, bgc);
-        }
-      }
+      if (!single) warp_sort_keys(keys, vals, m);
+      __syncwarp();
+      fold_sorted<T, FN, DEDUP>(keys, vals, m, c, last_part, bg, bgc);
       __syncwarp();
       lo_part = hi;
     }
@@ -505,54 +625,73 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
 // Integer `count` with background 0 (and float count with background 0 or
 // NaN) equals the pixel's coverage depth: every write after the first adds
 // one and no intermediate count can equal the background.  `any` is 1
-// wherever the depth is non-zero.  Neither needs values or order: one warp
-// per bucket adds every record's mask bits into per-pixel depths (lane l
-// owns pixel l of every word).
+// wherever the depth is non-zero.  Neither needs values or order.  One warp
+// per bucket (32 consecutive buckets per task, the next bucket's records
+// loaded while the current one is counted); for each word the records of
+// that word are found with a ballot and lane l adds their bit l.
 constexpr int DEPTH_WARPS = 8;
 
 template <typename T, int FN>
 __global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
-  __shared__ unsigned s_depth[DEPTH_WARPS][TW];
   const Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned* depth = s_depth[warp];
   const T bg = from_bits<T>(a.bg);
   T* out = static_cast<T*>(a.out);
+  const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
   const unsigned long long nwarps = (unsigned long long)gridDim.x * DEPTH_WARPS;
-  for (unsigned long long b = (unsigned long long)blockIdx.x * DEPTH_WARPS + warp; b < a.nbuckets; b += nwarps) {
-    const unsigned o0 = a.offsets[b];
-    const int n = (int)(a.offsets[b + 1] - o0);
-    const unsigned rowid = (unsigned)b / a.ntx;
-    const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
-    const int len = min(TW, a.ncols - c0);
-    T* dst = out + (unsigned long long)rowid * (unsigned long long)a.ncols + c0;
-    if (n == 0) {
-      store_bg<T>(dst, len, a.bg16, bg, lane, 32);
-      continue;
-    }
-#pragma unroll
-    for (int w = 0; w < WPT; ++w) depth[w * 32 + lane] = 0u;
-    for (int i0 = 0; i0 < n; i0 += 32) {
-      uint2 r = make_uint2(0u, 0u);
-      if (i0 + lane < n) r = a.recs[o0 + i0 + lane];
-      const int jn = min(32, n - i0);
-      for (int j = 0; j < jn; ++j) {
-        const unsigned rx = __shfl_sync(0xFFFFFFFFu, r.x, j), ry = __shfl_sync(0xFFFFFFFFu, r.y, j);
-        const int w = (int)((rx >> REC_W_SHIFT) & 15u);
-        depth[w * 32 + lane] += (ry >> lane) & 1u;
+  for (unsigned long long ch = (unsigned long long)blockIdx.x * DEPTH_WARPS + warp; ch < nchunks; ch += nwarps) {
+    const unsigned long long b0 = ch * FILL_CHUNK;
+    const int nb = (int)min((unsigned long long)FILL_CHUNK, a.nbuckets - b0);
+    const unsigned off = a.offsets[b0 + (lane < nb ? lane : nb)];
+    const unsigned off_end = a.offsets[b0 + nb];
+    unsigned o_next = __shfl_sync(0xFFFFFFFFu, off, 0);
+    unsigned e_next = nb > 1 ? __shfl_sync(0xFFFFFFFFu, off, 1) : off_end;
+    uint2 nxt = lane < (int)(e_next - o_next) ? a.recs[o_next + lane] : make_uint2(0u, 0u);
+    for (int k = 0; k < nb; ++k) {
+      const unsigned long long b = b0 + k;
+      const unsigned o0 = o_next, o1 = e_next;
+      const int n = (int)(o1 - o0);
+      uint2 r = nxt;
+      if (k + 1 < nb) {
+        o_next = __shfl_sync(0xFFFFFFFFu, off, k + 1);
+        e_next = k + 2 < nb ? __shfl_sync(0xFFFFFFFFu, off, (k + 2) & 31) : off_end;
+        nxt = lane < (int)(e_next - o_next) ? a.recs[o_next + lane] : make_uint2(0u, 0u);
       }
-    }
-#pragma unroll
-    for (int w = 0; w < WPT; ++w) {
-      const unsigned d = depth[w * 32 + lane];
-      T v = bg;
-      if (d) {
-        if constexpr (FN == F_ANY) v = T(1);
-        else if constexpr (std::is_integral<T>::value) v = (T)(typename std::make_unsigned<T>::type)d;
-        else v = (T)d;
+      const unsigned rowid = (unsigned)b / a.ntx;
+      const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
+      const int len = min(TW, a.ncols - c0);
+      T* dst = out + (unsigned long long)rowid * (unsigned long long)a.ncols + c0;
+      if (n == 0) {
+        store_bg<T>(dst, len, a.bg16, bg, lane, 32);
+        continue;
       }
-      if (w * 32 + lane < len) dst[w * 32 + lane] = v;
+      unsigned d[WPT];
+#pragma unroll
+      for (int w = 0; w < WPT; ++w) d[w] = 0u;
+      for (int i0 = 0; i0 < n; i0 += 32) {
+        if (i0 > 0) r = i0 + lane < n ? a.recs[o0 + i0 + lane] : make_uint2(0u, 0u);
+        const unsigned w_of = i0 + lane < n ? (r.x >> REC_W_SHIFT) & 15u : 16u;
+#pragma unroll
+        for (int w = 0; w < WPT; ++w) {
+          unsigned g = __ballot_sync(0xFFFFFFFFu, w_of == (unsigned)w);
+          while (g) {
+            const int src = __ffs(g) - 1;
+            g &= g - 1;
+            d[w] += (__shfl_sync(0xFFFFFFFFu, r.y, src) >> lane) & 1u;
+          }
+        }
+      }
+#pragma unroll
+      for (int w = 0; w < WPT; ++w) {
+        T v = bg;
+        if (d[w]) {
+          if constexpr (FN == F_ANY) v = T(1);
+          else if constexpr (std::is_integral<T>::value) v = (T)(typename std::make_unsigned<T>::type)d[w];
+          else v = (T)d[w];
+        }
+        if (w * 32 + lane < len) dst[w * 32 + lane] = v;
+      }
     }
   }
 }
@@ -581,7 +720,7 @@ int launch_fill_t(const FillArgs& a, int fn, bool dedup, int num_sms, cudaStream
 #define RZ_FILL_CASE(FNV, DD)                                                                             \
   {                                                                                                       \
     constexpr int ws = FILL_WARPS_PER_BLOCK * fill_warp_bytes<T>();                                       \
-    constexpr int bs = BIG_WARPS * big_warp_bytes();                                                      \
+    constexpr int bs = BIG_WARPS * big_warp_bytes<T>();                                                   \
     cudaFuncSetAttribute(k_fill_warp<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws);       \
     cudaFuncSetAttribute(k_fill_big<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, bs);        \
     unsigned long long want = (a.nbuckets + FILL_WARPS_PER_BLOCK - 1) / FILL_WARPS_PER_BLOCK;             \

@@ -9,6 +9,8 @@
 //   rasterization/burn_geometry.rs   part semantics (pooled rings / edges)
 #pragma once
 
+#include <type_traits>
+
 #include "rz_device.cuh"
 #include "rz_poly.cuh"
 
@@ -359,12 +361,18 @@ __global__ void k_point_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan
 
 // ------------------------------------------------------------- scatter -----
 // Move each coverage record into its bucket's range as {part | word-in-tile
-// << REC_W_SHIFT | DEDUP_BIT, mask}.  Order inside a bucket is arbitrary
-// here; the fill kernels restore part order.  Records of one bucket that
-// sit in one warp (neighbouring words of a row) take their slots with one
-// atomic.
+// << REC_W_SHIFT | DEDUP_BIT, mask}, and its part's burn value (VB bytes,
+// values[part_geom[part]]) beside it, so the fill reads both with one
+// dependent load.  Order inside a bucket is arbitrary here; the fill kernels
+// restore part order.  Records of one bucket that sit in one warp
+// (neighbouring words of a row) take their slots with one atomic.
+template <int VB>
 __global__ void k_scatter(RecBuf sb, const unsigned* __restrict__ offsets, unsigned* counts, uint2* sorted,
+                          const void* __restrict__ values, const unsigned* __restrict__ part_geom, void* rvals,
                           Ctrl* ctrl) {
+  using V = typename std::conditional<VB == 1, unsigned char,
+            typename std::conditional<VB == 2, unsigned short,
+            typename std::conditional<VB == 4, unsigned, unsigned long long>::type>::type>::type;
   if (ctrl->err || ctrl->span_count > sb.cap) return;
   const unsigned long long n = ctrl->span_count;
   const int lane = threadIdx.x & 31;
@@ -377,13 +385,15 @@ __global__ void k_scatter(RecBuf sb, const unsigned* __restrict__ offsets, unsig
     const unsigned b = valid ? wid / WPT : 0xFFFFFFFFu;
     const unsigned same = __match_any_sync(0xFFFFFFFFu, b);
     const int leader = __ffs(same) - 1;
-    unsigned top = 0;
-    if (valid && lane == leader) top = atomicSub(&counts[b], (unsigned)__popc(same));
-    top = __shfl_sync(0xFFFFFFFFu, top, leader);
+    unsigned left = 0;  // records of the bucket not placed yet, before this group
+    if (valid && lane == leader) left = atomicSub(&counts[b], (unsigned)__popc(same));
+    left = __shfl_sync(0xFFFFFFFFu, left, leader);
     if (valid) {
+      const unsigned part = sb.part[i];
       const unsigned rank = (unsigned)__popc(same & ((1u << lane) - 1u));
-      const unsigned pos = offsets[b] + top - 1u - rank;
-      sorted[pos] = make_uint2(sb.part[i] | ((wid % WPT) << REC_W_SHIFT), sb.mask[i]);
+      const unsigned pos = offsets[b + 1] - left + rank;  // arrival order
+      sorted[pos] = make_uint2(part | ((wid % WPT) << REC_W_SHIFT), sb.mask[i]);
+      if (values) static_cast<V*>(rvals)[pos] = static_cast<const V*>(values)[part_geom[part & REC_PART_MASK]];
     }
   }
 }
