@@ -47,10 +47,11 @@ constexpr int SMALL_WARPS = 4;  // warps (independent windows) per block
 constexpr int SMALL_WARP_SMEM = POLY_WARP_QCAP * POLY_QENT + SMALL_BITMAP_WORDS * 4 + 3 * WR_MAX * 4 + 16;
 constexpr int SMALL_SMEM = SMALL_WARPS * SMALL_WARP_SMEM;
 
-// Fill: buckets with at most FILL_WARP_MAX records are sorted and applied by
+// Fill: buckets with at most FILL_WARP_SORT records are sorted and applied by
 // one warp; larger ones go to the per-word path, which takes at most
 // BIG_CAP records of one word at a time.
-constexpr int FILL_WARP_MAX = 64;
+constexpr int FILL_WARP_MAX = 64;    // records held in registers (two per lane)
+constexpr int FILL_WARP_SORT = 256;  // records sorted in shared memory by one warp
 // Bytes of record scratch per record: 12 before the scatter, 8 after it and
 // 8 for its value.
 constexpr size_t RECORD_BYTES = 28;
@@ -80,7 +81,8 @@ struct Ctrl {
   unsigned int err;
   unsigned int big_count;
   unsigned long long work_small;  // narrow-part polygon window work counter
-  unsigned long long pad[9];
+  unsigned long long fill_work;    // fill kernels: chunk / item counter
+  unsigned long long pad[8];
 };
 
 struct Grid {

@@ -223,6 +223,7 @@ __global__ void k_reset_pass(Ctrl* c) {
   c->work = 0;
   c->work_small = 0;
   c->big_count = 0;
+  c->fill_work = 0;
 }
 
 extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void* values, const void* background,

@@ -235,7 +235,7 @@ constexpr int FILL_CHUNK = 32;
 
 template <typename T>
 constexpr int fill_warp_bytes() {
-  return FILL_WARP_MAX * (int)sizeof(SRec);
+  return FILL_WARP_SORT * ((int)sizeof(SRec) + 8);
 }
 
 // the two records (positions lane and lane + 32) of a bucket held by a lane
@@ -308,10 +308,73 @@ __device__ __forceinline__ void warp_sort64(unsigned& k0, unsigned& i0, unsigned
   }
 }
 
+// ascending bitonic sort of k[0..np) (np = next power of two >= n, padded
+// with ~0) by one warp in shared memory
+__device__ __forceinline__ void warp_sort_u64(unsigned long long* k, int n) {
+  int np = 1;
+  while (np < n) np <<= 1;
+  const int lane = threadIdx.x & 31;
+  for (int i = n + lane; i < np; i += 32) k[i] = ~0ull;
+  __syncwarp();
+  for (int kk = 2; kk <= np; kk <<= 1) {
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < np; i += 32) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const unsigned long long x = k[i], y = k[ixj];
+          const bool up = (i & kk) == 0;
+          if ((x > y) == up) {
+            k[i] = y;
+            k[ixj] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Walk n records in (word, part) order -- srec itself, or srec[skey[p] & 0xFF]
+// when a sorted key array is given -- and write the tile: lane l folds pixel
+// l of the current word and stores the word when the walk moves on; words
+// without records are background.
+template <typename T, int FN, bool DEDUP>
+__device__ __forceinline__ void fold_words(const SRec* srec, const unsigned long long* skey, int n, T* dst, int len,
+                                           T bg, const BgF64& bgc) {
+  const int lane = threadIdx.x & 31;
+  int cw = -1;
+  T c = bg;
+  unsigned prev_key = 0xFFFFFFFFu, seen = 0u;
+  for (int p = 0; p < n; ++p) {
+    const SRec e = skey ? srec[(unsigned)skey[p] & 0xFFu] : srec[p];
+    const int w = (int)((e.key >> REC_W_SHIFT) & 15u);
+    if (w != cw) {
+      if (cw >= 0 && cw * 32 + lane < len) dst[cw * 32 + lane] = c;
+      for (int ww = cw + 1; ww < w; ++ww)
+        if (ww * 32 + lane < len) dst[ww * 32 + lane] = bg;
+      cw = w;
+      c = bg;
+      prev_key = 0xFFFFFFFFu;
+    }
+    unsigned mask = e.mask;
+    if (DEDUP && (e.key & DEDUP_BIT)) {
+      const unsigned key = e.key & ~DEDUP_BIT;
+      if (key != prev_key) seen = 0u;
+      mask &= ~seen;
+      seen |= e.mask;
+      prev_key = key;
+    }
+    apply_step<T, FN>(c, from_bits<T>(e.vbits), (mask >> lane) & 1u, bg, bgc);
+  }
+  if (cw * 32 + lane < len) dst[cw * 32 + lane] = c;
+  for (int ww = cw + 1; ww < WPT; ++ww)
+    if (ww * 32 + lane < len) dst[ww * 32 + lane] = bg;
+}
+
 template <typename T, int FN, bool DEDUP>
 __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Ctrl* ctrl = a.ctrl;
+  Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   SRec* srec = reinterpret_cast<SRec*>(smem + warp * fill_warp_bytes<T>());
@@ -319,9 +382,11 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
   const BgF64 bgc = bg_f64(a.bg);
   T* out = static_cast<T*>(a.out);
   const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
-  const unsigned long long nwarps = (unsigned long long)gridDim.x * FILL_WARPS_PER_BLOCK;
-  for (unsigned long long ch = (unsigned long long)blockIdx.x * FILL_WARPS_PER_BLOCK + warp; ch < nchunks;
-       ch += nwarps) {
+  while (true) {
+    unsigned long long ch = 0;
+    if (lane == 0) ch = atomicAdd(&a.ctrl->fill_work, 1ull);
+    ch = __shfl_sync(0xFFFFFFFFu, ch, 0);
+    if (ch >= nchunks) break;
     const unsigned long long b0 = ch * FILL_CHUNK;
     const int nb = (int)min((unsigned long long)FILL_CHUNK, a.nbuckets - b0);
     const unsigned off = a.offsets[b0 + (lane < nb ? lane : nb)];
@@ -332,6 +397,7 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
     for (int k = 0; k < nb; ++k) {
       const unsigned long long b = b0 + k;
       const int n = n_next;
+      const unsigned o_cur = o_next;
       const LanePair<T> pr = nxt;
       if (k + 1 < nb) {  // prefetch the next bucket
         o_next = __shfl_sync(0xFFFFFFFFu, off, k + 1);
@@ -347,7 +413,26 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
         continue;
       }
       if (n > FILL_WARP_MAX) {
-        if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
+        if (n > FILL_WARP_SORT) {
+          if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
+          continue;
+        }
+        // up to FILL_WARP_SORT records: staged and sorted in shared memory,
+        // key = (word, part) << 8 | position
+        const unsigned o0 = o_cur;
+        unsigned long long* skey = reinterpret_cast<unsigned long long*>(srec + FILL_WARP_SORT);
+        for (int i = lane; i < n; i += 32) {
+          const uint2 r = a.recs[o0 + i];
+          SRec e;
+          e.key = r.x;
+          e.mask = r.y;
+          e.vbits = to_bits<T>(rec_value<T>(a, o0 + i));
+          srec[i] = e;
+          skey[i] = ((unsigned long long)(r.x & ~DEDUP_BIT) << 8) | (unsigned)i;
+        }
+        warp_sort_u64(skey, n);
+        fold_words<T, FN, DEDUP>(srec, skey, n, dst, len, bg, bgc);
+        __syncwarp();
         continue;
       }
       // (word, part) keys; invalid positions sort last
@@ -392,34 +477,7 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
         }
       }
       __syncwarp();
-      // walk the records once; lane l folds pixel l of the current word
-      int cw = -1;
-      T c = bg;
-      unsigned prev_key = 0xFFFFFFFFu, seen = 0u;
-      for (int p = 0; p < n; ++p) {
-        const SRec e = srec[p];
-        const int w = (int)((e.key >> REC_W_SHIFT) & 15u);
-        if (w != cw) {
-          if (cw >= 0 && cw * 32 + lane < len) dst[cw * 32 + lane] = c;
-          for (int ww = cw + 1; ww < w; ++ww)
-            if (ww * 32 + lane < len) dst[ww * 32 + lane] = bg;
-          cw = w;
-          c = bg;
-          prev_key = 0xFFFFFFFFu;
-        }
-        unsigned mask = e.mask;
-        if (DEDUP && (e.key & DEDUP_BIT)) {
-          const unsigned key = e.key & ~DEDUP_BIT;
-          if (key != prev_key) seen = 0u;
-          mask &= ~seen;
-          seen |= e.mask;
-          prev_key = key;
-        }
-        apply_step<T, FN>(c, from_bits<T>(e.vbits), (mask >> lane) & 1u, bg, bgc);
-      }
-      if (cw * 32 + lane < len) dst[cw * 32 + lane] = c;
-      for (int ww = cw + 1; ww < WPT; ++ww)
-        if (ww * 32 + lane < len) dst[ww * 32 + lane] = bg;
+      fold_words<T, FN, DEDUP>(srec, (const unsigned long long*)nullptr, n, dst, len, bg, bgc);
       __syncwarp();
     }
   }
@@ -633,14 +691,17 @@ constexpr int DEPTH_WARPS = 8;
 
 template <typename T, int FN>
 __global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
-  const Ctrl* ctrl = a.ctrl;
+  Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const T bg = from_bits<T>(a.bg);
   T* out = static_cast<T*>(a.out);
   const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
-  const unsigned long long nwarps = (unsigned long long)gridDim.x * DEPTH_WARPS;
-  for (unsigned long long ch = (unsigned long long)blockIdx.x * DEPTH_WARPS + warp; ch < nchunks; ch += nwarps) {
+  while (true) {
+    unsigned long long ch = 0;
+    if (lane == 0) ch = atomicAdd(&a.ctrl->fill_work, 1ull);
+    ch = __shfl_sync(0xFFFFFFFFu, ch, 0);
+    if (ch >= nchunks) break;
     const unsigned long long b0 = ch * FILL_CHUNK;
     const int nb = (int)min((unsigned long long)FILL_CHUNK, a.nbuckets - b0);
     const unsigned off = a.offsets[b0 + (lane < nb ? lane : nb)];
@@ -708,12 +769,26 @@ bool depth_exact(const FillArgs& a, int fn, bool dedup) {
 
 template <typename T>
 int launch_fill_t(const FillArgs& a, int fn, bool dedup, int num_sms, cudaStream_t s) {
+  // persistent grids: as many blocks as fit on the GPU at once, chunks of
+  // buckets handed out by an atomic counter
+  const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
+  auto persistent = [&](const void* kern, int threads, int smem_bytes, int per_block_units) {
+    int bps = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, threads, smem_bytes);
+    if (bps < 1) bps = 1;
+    unsigned long long want = (nchunks + per_block_units - 1) / per_block_units;
+    unsigned long long g = (unsigned long long)num_sms * bps;
+    if (want < g) g = want;
+    return (unsigned)(g ? g : 1);
+  };
   if (depth_exact<T>(a, fn, dedup)) {
-    unsigned long long want = (a.nbuckets + DEPTH_WARPS - 1) / DEPTH_WARPS;
-    unsigned grid = (unsigned)(want < (unsigned long long)num_sms * 16 ? want : num_sms * 16ull);
-    if (grid == 0) grid = 1;
-    if (fn == F_ANY) k_fill_depth<T, F_ANY><<<grid, DEPTH_WARPS * 32, 0, s>>>(a);
-    else k_fill_depth<T, F_COUNT><<<grid, DEPTH_WARPS * 32, 0, s>>>(a);
+    if (fn == F_ANY) {
+      const unsigned grid = persistent((const void*)k_fill_depth<T, F_ANY>, DEPTH_WARPS * 32, 0, DEPTH_WARPS);
+      k_fill_depth<T, F_ANY><<<grid, DEPTH_WARPS * 32, 0, s>>>(a);
+    } else {
+      const unsigned grid = persistent((const void*)k_fill_depth<T, F_COUNT>, DEPTH_WARPS * 32, 0, DEPTH_WARPS);
+      k_fill_depth<T, F_COUNT><<<grid, DEPTH_WARPS * 32, 0, s>>>(a);
+    }
     return 1;
   }
   int launches = 0;
@@ -723,9 +798,8 @@ int launch_fill_t(const FillArgs& a, int fn, bool dedup, int num_sms, cudaStream
     constexpr int bs = BIG_WARPS * big_warp_bytes<T>();                                                   \
     cudaFuncSetAttribute(k_fill_warp<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws);       \
     cudaFuncSetAttribute(k_fill_big<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, bs);        \
-    unsigned long long want = (a.nbuckets + FILL_WARPS_PER_BLOCK - 1) / FILL_WARPS_PER_BLOCK;             \
-    unsigned grid = (unsigned)(want < (unsigned long long)num_sms * 16 ? want : num_sms * 16ull);         \
-    if (grid == 0) grid = 1;                                                                              \
+    const unsigned grid =                                                                                 \
+        persistent((const void*)k_fill_warp<T, FNV, DD>, FILL_WARPS_PER_BLOCK * 32, ws, FILL_WARPS_PER_BLOCK); \
     k_fill_warp<T, FNV, DD><<<grid, FILL_WARPS_PER_BLOCK * 32, ws, s>>>(a);                               \
     k_fill_big<T, FNV, DD><<<num_sms * 4, BIG_WARPS * 32, bs, s>>>(a);                                    \
     launches += 2;                                                                                        \
