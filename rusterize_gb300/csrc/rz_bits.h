@@ -170,108 +170,157 @@ RZ_HD float f32_add(float a, float b) { return __fadd_rn(a, b); }
 RZ_HD float f32_sub(float a, float b) { return __fsub_rn(a, b); }
 RZ_HD float f32_mul(float a, float b) { return __fmul_rn(a, b); }
 RZ_HD float f32_div(float a, float b) { return __fdiv_rn(a, b); }
+RZ_HD float f32_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 RZ_HD float f32_floor(float a) { return floorf(a); }
 RZ_HD float f32_abs(float a) { return fabsf(a); }
 RZ_HD float f32_inf() { return __int_as_float(0x7F800000); }
+// a / b within 2 ulp (|b| in [2^-126, 2^126])
+RZ_HD float f32_div_fast(float a, float b) { return __fdividef(a, b); }
 #else
 RZ_HD float f32_add(float a, float b) { return a + b; }
 RZ_HD float f32_sub(float a, float b) { return a - b; }
 RZ_HD float f32_mul(float a, float b) { return a * b; }
 RZ_HD float f32_div(float a, float b) { return a / b; }
+RZ_HD float f32_fma(float a, float b, float c) { return __builtin_fmaf(a, b, c); }
 RZ_HD float f32_floor(float a) { return __builtin_floorf(a); }
 RZ_HD float f32_abs(float a) { return __builtin_fabsf(a); }
 RZ_HD float f32_inf() { return __builtin_inff(); }
+// Host stand-in for the device's 2-ulp division: the correctly rounded
+// quotient moved by up to 2 ulp (chosen from the operand bits), so host tests
+// exercise the error bound with the device's worst case.
+RZ_HD float f32_div_fast(float a, float b) {
+  float q = a / b;
+  uint32_t ua, ub;
+  memcpy(&ua, &a, 4);
+  memcpy(&ub, &b, 4);
+  const int k = (int)(((ua * 2654435761u) ^ (ub * 40503u)) >> 29) % 5 - 2;  // -2..2
+  for (int i = 0; i < (k < 0 ? -k : k); ++i) q = __builtin_nextafterf(q, k < 0 ? -__builtin_inff() : __builtin_inff());
+  return q;
+}
 #endif
 
 // Largest pixel coordinate magnitude handled by the filter (2^22): integer
 // parts and their differences stay exact in FP32 and every crossing value
 // stays below 2^23, where FP32 still resolves fractions.
 constexpr int CROSS_COORD_LOG2 = 22;
-constexpr float CROSS_ULP = 2.384185791015625e-07f;  // 2^-22, the unit of the bound
+
+RZ_HD uint32_t funnel_r(uint32_t lo, uint32_t hi, int sh) {  // low word of (hi:lo) >> sh, 0 <= sh < 32
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_r(lo, hi, (unsigned)sh);
+#else
+  return (uint32_t)((((uint64_t)hi << 32) | lo) >> sh);
+#endif
+}
 
 // c ~ ci + cf with |c - (ci + cf)| < 2^-23, cf in [0, 1) and ci = floor(c)
-// (or floor(c) + 1 for a negative c within 2^-40 below an integer); false
-// for |c| >= 2^22, infinities and NaN.  |c| is truncated to a fixed-point
-// number with 40 fraction bits (error < 2^-40) and given c's sign; its
-// integer part (arithmetic shift) is ci and its top 24 fraction bits become
-// cf (error < 2^-24).
-RZ_HD bool split_px(double c, int& ci, float& cf) {
+// (or floor(c) + 1 for a negative c within 2^-24 below an integer); false
+// for |c| >= 2^22, infinities and NaN.  The integer part of |c| and the top
+// 24 bits of its fraction (truncated: error < 2^-24) come from funnel shifts
+// of the significand's two 32-bit halves; a negative c becomes
+// -(int part) - 1 and 1 - fraction.  *f24 (when given) receives the 24
+// fraction bits of a non-negative c, before the sign is applied.
+RZ_HD bool split_px(double c, int& ci, float& cf, uint32_t* f24_out = nullptr) {
   const uint64_t b = f64_bits(c);
-  const int E = (int)((b >> 52) & 0x7FF);
+  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  const int E = (int)((hi >> 20) & 0x7FF);
   if (E >= 1023 + CROSS_COORD_LOG2) {
     ci = 0;
     cf = 0.0f;
     return false;
   }
-  const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
-  const int sh = E - 1023 - 12;  // |c| * 2^40 = m * 2^sh
-  uint64_t q = 0;
-  if (E != 0) {
-    if (sh >= 0) q = m << sh;
-    else if (sh > -64) q = m >> (-sh);
+  const uint32_t mh = (hi & 0xFFFFFu) | 0x100000u;  // significand bits 52..32
+  uint32_t ip = 0, f24 = 0;
+  if (E >= 1023) {  // 1 <= |c| < 2^22: the binary point sits s = 52 - e bits up, s in [31, 52]
+    const int sh = 1075 - E;
+    ip = sh >= 32 ? mh >> (sh - 32) : funnel_r(lo, mh, sh);
+    f24 = funnel_r(lo, mh, sh - 24) & 0xFFFFFFu;
+  } else if (E >= 1023 - 30) {  // 2^-30 <= |c| < 1: |c| * 2^24 = significand >> (28 - e)
+    const int t = 1051 - E;     // in [29, 58]
+    f24 = t < 32 ? funnel_r(lo, mh, t) : mh >> (t - 32);
+  }                             // smaller magnitudes (and zero) split to 0 + 0
+  if (f24_out) *f24_out = f24;
+  if (hi >> 31) {
+    ci = f24 ? -(int)ip - 1 : -(int)ip;
+    f24 = f24 ? (1u << 24) - f24 : 0u;
+  } else {
+    ci = (int)ip;
   }
-  const int64_t sq = (b >> 63) ? -(int64_t)q : (int64_t)q;
-  ci = (int)(sq >> 40);  // arithmetic shift: floor
-  const uint32_t f24 = (uint32_t)(((uint64_t)sq & ((1ull << 40) - 1)) >> 16);
   cf = (float)f24 * 5.9604644775390625e-08f;  // * 2^-24, exact
   return true;
 }
 
-// One edge in the filter's frame.  ee = +inf marks an edge whose crossings
-// all take the FP64 sequence (non-finite or huge coordinates, or a nearly
+// clamp(ceil(fl(y - 0.5)), 0, hi) from y's split: for 0 <= y < 2^22 the
+// subtraction is exact and the ceiling is yi or yi + 1 depending on whether
+// the fraction is below or above one half; a fraction within 2^-24 of one
+// half (or a negative / unsplittable y) takes the exact path.
+RZ_HD int ceil_half_down_split(double y, bool ok, int yi, uint32_t f24, int hi) {
+  if (ok && yi >= 0 && f24 != (1u << 23)) {
+    const int r = yi + (f24 > (1u << 23) ? 1 : 0);
+    return r > hi ? hi : r;
+  }
+  return ceil_half_down(y, hi);
+}
+
+// One edge in the filter's frame, for the crossings of rows row0, row0 + 1,
+// ... of one scanline window.  e0 = +inf marks an edge whose crossings all
+// take the FP64 sequence (non-finite or huge coordinates, or a nearly
 // horizontal edge: those have at most one crossing).
 struct CrossEdge {
-  int xi, yi;   // floor of x_top, y_top
-  float xf;     // x_top - xi
-  float g0;     // 0.5 - (y_top - yi)
-  float a;      // dxdy
-  float ee;     // per-edge part of the error bound, in units of 2^-22
+  int xi;      // floor of x_top (split)
+  float d0;    // (row0 + 0.5) - y_top
+  float a;     // dxdy
+  float c0;    // (x_top - xi) + 0.5
+  float e0;    // error bound E of every crossing of the edge
+  float e1;    // 1 - E
 };
 
-// The edge from top end (xti + xtf, yti + ytf) to bottom end (xbi + xbf,
-// ybi + ybf), each given by split_px; `ok` is false when a split failed.
+// Error of a crossing (row row0 + j, value t = fl(fl(d0 + j) * a + c0) with
+// one FMA rounding, relative to xi), in units of u = 2^-24, the FP32 unit
+// roundoff (split errors < 2u, the slope division < 4u relative, |d| <= dy
+// because the row is a crossing row of the edge):
+//   offset d:          2.5 + 2|d|          slope a: (5 + |dx| + 5|a| + |a dy|) / dy + 4|a|
+//   |d a - D* M*| <=   5 + 7.5|a| + 2|dx| + 6|p|      c0, the split of x, t: 3 + |t|
+//   the FP64 sequence and its +0.5 (|x| < 2^23):       0.5
+// and since the crossing lies between the edge's end points, |p| <= |dx|
+// and |t| <= |dx| + 1.5, so the total is below 28 + 7.5|a| + 15|dx|.  The
+// bound used, 2^-20 (32 + 8|a| + 16|dx|) = u (512 + 128|a| + 256|dx|), is
+// 16 times larger.
 RZ_HD void cross_edge_frame(int xti, float xtf, int yti, float ytf, int xbi, float xbf, int ybi, float ybf, bool ok,
-                            CrossEdge& e) {
+                            int row0, CrossEdge& e) {
   e.xi = xti;
-  e.yi = yti;
-  e.xf = xtf;
   // integer parts differ by < 2^23: exact in FP32
   const float dx = f32_add((float)(xbi - xti), f32_sub(xbf, xtf));
   const float dy = f32_add((float)(ybi - yti), f32_sub(ybf, ytf));
   ok = ok && dy >= 0.00390625f;  // y_bot - y_top >= 2^-8
-  e.a = ok ? f32_div(dx, dy) : 0.0f;
-  e.g0 = f32_sub(0.5f, ytf);
-  // error of the crossing, in units of 2^-24 (u = 2^-24 is the FP32 unit
-  // roundoff; the split errors are < 2u):
-  //   frame offsets and the f32 crossing:   <= 7.5 + 7.5|a| + 2|d a| + |dx| + |a dy| + |p| + |s| + |t|
-  //   the FP64 sequence and its +0.5:        <= 0.5 for |x| < 2^23
-  // with |d| <= dy, |d a| ~ |p| and |a dy| ~ |dx| this is below
-  // 8 + 8|a| + 2|dx| + 3|p| + 2|t|; the bound below uses 2^-22 units (4x).
-  e.ee = ok ? f32_add(f32_add(8.0f, f32_mul(8.0f, f32_abs(e.a))), f32_mul(2.0f, f32_abs(dx))) : f32_inf();
+  e.a = ok ? f32_div_fast(dx, dy) : 0.0f;
+  e.d0 = f32_add((float)(row0 - yti), f32_sub(0.5f, ytf));
+  e.c0 = f32_add(xtf, 0.5f);
+  const float E = f32_mul(9.5367431640625e-07f,  // 2^-20
+                          f32_add(f32_add(32.0f, f32_mul(8.0f, f32_abs(e.a))), f32_mul(16.0f, f32_abs(dx))));
+  e.e0 = ok ? E : f32_inf();
+  e.e1 = ok ? f32_sub(1.0f, E) : -f32_inf();
 }
 
-RZ_HD void cross_edge_setup(double xt, double yt, double xb, double yb, CrossEdge& e) {
+RZ_HD void cross_edge_setup(double xt, double yt, double xb, double yb, int row0, CrossEdge& e) {
   int xti, yti, xbi, ybi;
   float xtf, ytf, xbf, ybf;
   bool ok = split_px(xt, xti, xtf);
   ok = split_px(yt, yti, ytf) && ok;
   ok = split_px(xb, xbi, xbf) && ok;
   ok = split_px(yb, ybi, ybf) && ok;
-  cross_edge_frame(xti, xtf, yti, ytf, xbi, xbf, ybi, ybf, ok, e);
+  cross_edge_frame(xti, xtf, yti, ytf, xbi, xbf, ybi, ybf, ok, row0, e);
 }
 
 // Boundary clamp(floor(fl(x + 0.5)), 0, ncols) of the crossing with the
-// centre of row r, or -1 when the filter cannot decide it.  r must be a
-// crossing row of the edge (ceil(y_top - 0.5) <= r < ceil(y_bot - 0.5)).
-RZ_HD int cross_fast(const CrossEdge& e, int r, int ncols) {
-  const float d = f32_add((float)(r - e.yi), e.g0);
-  const float p = f32_mul(d, e.a);
-  const float s = f32_add(e.xf, p);
-  const float t = f32_add(s, 0.5f);
+// centre of row row0 + j, or -1 when the filter cannot decide it.  The row
+// must be a crossing row of the edge (ceil(y_top - 0.5) <= row <
+// ceil(y_bot - 0.5)) and j < 2^24.
+RZ_HD int cross_fast(const CrossEdge& e, int j, int ncols) {
+  const float d = f32_add(e.d0, (float)j);
+  const float t = f32_fma(d, e.a, e.c0);
   const float fl = f32_floor(t);
   const float fr = f32_sub(t, fl);
-  const float E = f32_mul(CROSS_ULP, f32_add(e.ee, f32_add(f32_mul(3.0f, f32_abs(p)), f32_mul(2.0f, f32_abs(t)))));
-  if (!(fr >= E && fr <= f32_sub(1.0f, E))) return -1;
+  if (!(fr >= e.e0 && fr <= e.e1)) return -1;
   const int bnd = e.xi + (int)fl;
   return bnd < 0 ? 0 : (bnd > ncols ? ncols : bnd);
 }

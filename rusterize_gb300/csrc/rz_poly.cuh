@@ -47,14 +47,15 @@ namespace rzd {
 
 // One queued edge in the crossing filter's frame (CrossEdge, rz_bits.h).
 struct __align__(16) QEnt {
-  int xi, yi;
-  float xf, g0, a, ee;
+  int xi;
+  float d0, a, c0, e0, e1;
   unsigned v;     // first vertex of the edge, relative to the part | top flag (bit 31)
   unsigned rows;  // first row - r0 (bits 0-7) | row count (bits 8-15)
 };
 static_assert(sizeof(QEnt) == 32, "queue entry layout");
 
 constexpr int QCAP = POLY_WARP_QCAP;
+constexpr int NARROW_CHUNK = 4;  // narrow windows per work item
 constexpr int STAGE_CAP = (QCAP * 32) / 12 / 8 * 8;  // staged records per warp (aliases the queue)
 
 struct PolyWin {
@@ -124,21 +125,22 @@ __device__ __forceinline__ void warp_cross(const Geo& geo, const Grid& g, const 
       const int m = m0 + lane;
       if (m >= total) continue;
       const QEnt qe = q[base + s];
-      const int row = w.r0 + (int)(qe.rows & 0xFFu) + (m - es);
+      const int j = m - es;
+      const int rowrel = (int)(qe.rows & 0xFFu) + j;
+      const int row = w.r0 + rowrel;
       CrossEdge ce;
       ce.xi = qe.xi;
-      ce.yi = qe.yi;
-      ce.xf = qe.xf;
-      ce.g0 = qe.g0;
+      ce.d0 = qe.d0;
       ce.a = qe.a;
-      ce.ee = qe.ee;
-      int r = cross_fast(ce, row, g.ncols);
+      ce.c0 = qe.c0;
+      ce.e0 = qe.e0;
+      ce.e1 = qe.e1;
+      int r = cross_fast(ce, j, g.ncols);
       if (r < 0) {
         r = cross_exact(geo, g, vs + (qe.v & 0x7FFFFFFFu), qe.v >> 31, row);
         if (r < 0) continue;
       }
       const int loc = r - w.col0;
-      const int rowrel = row - w.r0;
       if (loc < 0 || loc >= w.nbits) {
         set_error(ctrl, ERR_BITMAP, part);
         continue;
@@ -165,10 +167,11 @@ struct VtxState {
 __device__ __forceinline__ VtxState vtx_state(const Grid& g, double2 w) {
   VtxState s;
   s.py = to_py(g, w.y);
-  s.ys = row_ceil(s.py, g.nrows);
+  uint32_t yf24 = 0;
+  const bool oky = rzb::split_px(s.py, s.yi, s.yf, &yf24);
+  s.ys = rzb::ceil_half_down_split(s.py, oky, s.yi, yf24, g.nrows);  // edges.rs:32-33
   const double px = to_px(g, w.x);
   const bool okx = rzb::split_px(px, s.xi, s.xf);
-  const bool oky = rzb::split_px(s.py, s.yi, s.yf);
   s.ok = okx && oky;
   return s;
 }
@@ -204,6 +207,10 @@ __device__ __forceinline__ void warp_pass(const Geo& geo, const Grid& g, unsigne
   const int lane = threadIdx.x & 31;
   if (vb >= ve) return;
   const double2* xy = geo.xy + vs;
+  // pull the warp's vertex range into L2 (one 128-byte line per lane and
+  // instruction), so that the one-chunk-ahead loads below hit L2
+  for (unsigned off = vb * 16u + (unsigned)lane * 128u; off < ve * 16u; off += 32u * 128u)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char*>(xy) + off));
   const unsigned nring = (unsigned)(re - rb);
   const bool few = nring <= 32;
   unsigned rend = 0xFFFFFFFFu;  // lane j: end (exclusive) of ring rb + j = start of the next ring
@@ -262,13 +269,13 @@ __device__ __forceinline__ void warp_pass(const Geo& geo, const Grid& g, unsigne
           const VtxState& t = top0 ? prv : cur;
           const VtxState& bt = top0 ? cur : prv;
           CrossEdge ce;
-          rzb::cross_edge_frame(t.xi, t.xf, t.yi, t.yf, bt.xi, bt.xf, bt.yi, bt.yf, t.ok && bt.ok, ce);
+          rzb::cross_edge_frame(t.xi, t.xf, t.yi, t.yf, bt.xi, bt.xf, bt.yi, bt.yf, t.ok && bt.ok, a, ce);
           e.xi = ce.xi;
-          e.yi = ce.yi;
-          e.xf = ce.xf;
-          e.g0 = ce.g0;
+          e.d0 = ce.d0;
           e.a = ce.a;
-          e.ee = ce.ee;
+          e.c0 = ce.c0;
+          e.e0 = ce.e0;
+          e.e1 = ce.e1;
           e.v = (v - 1) | (top0 ? 0x80000000u : 0u);
           e.rows = (unsigned)(a - w.r0) | ((unsigned)(b - a) << 8);
           push = true;
@@ -462,12 +469,21 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
   const unsigned long long total = poff[geo.n_parts * PC_N + PC_WIN_SMALL];
   unsigned long long ncross = 0, npix = 0;
   int st_n = 0;
+  unsigned long long wi = 0, wend = 0, p = 0;
   while (true) {
-    unsigned long long wi = 0;
-    if (lane == 0) wi = atomicAdd(&ctrl->work_small, 1ull);
-    wi = __shfl_sync(0xFFFFFFFFu, wi, 0);
-    if (wi >= total) break;
-    const unsigned long long p = window_part(poff, PC_WIN_SMALL, geo.n_parts, wi);
+    // windows are taken NARROW_CHUNK at a time: the part of the first is
+    // searched, the following ones walk forward from it
+    if (wi >= wend) {
+      unsigned long long c0 = 0;
+      if (lane == 0) c0 = atomicAdd(&ctrl->work_small, (unsigned long long)NARROW_CHUNK);
+      c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
+      if (c0 >= total) break;
+      wi = c0;
+      wend = min(total, c0 + NARROW_CHUNK);
+      p = window_part(poff, PC_WIN_SMALL, geo.n_parts, wi);
+    } else {
+      while (poff[(p + 1) * PC_N + PC_WIN_SMALL] <= wi) ++p;
+    }
     const PartPlan pl = plan[p];
     const int k = (int)(wi - poff[p * PC_N + PC_WIN_SMALL]);
     const PolyWin win = make_window(pl, k);
@@ -496,6 +512,7 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
     }
     warp_extract(bm, nr, bw, win.r0, win.col0, pl.band, (unsigned)p, g, ws, st_n, sb, bucket_count, ctrl, npix);
     stage_flush(ws, st_n, sb, bucket_count, ctrl);  // the stage aliases the queue of the next window
+    ++wi;
   }
   flush_counters(ncross, npix, ctrl);
 }

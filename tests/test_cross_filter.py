@@ -42,16 +42,20 @@ static void check_edge(double x0, double y0, double x1, double y1, int ncols, in
   if (!(ye > 0.0)) return;
   long rs = ys < 0 ? 0 : (long)ys, re = (long)ye;
   if (re <= rs) return;
+  // the frame is set up for a window starting at row0 (the edge's first
+  // row, or a later one as when a tall edge spans several windows)
+  long row0 = rs;
+  if (re - rs > 4 && (rng() & 1)) row0 = rs + (long)(rng() % (uint64_t)(re - rs));
   rzb::CrossEdge e;
-  rzb::cross_edge_setup(xt, yt, xb, yb, e);
+  rzb::cross_edge_setup(xt, yt, xb, yb, (int)row0, e);
   const double dxdy = (xb - xt) / (yb - yt);
-  long nrow = re - rs;
+  long nrow = re - row0;
   for (int k = 0; k < max_rows && k < nrow; ++k) {
-    long r = nrow <= max_rows ? rs + k : rs + (long)(rng() % (uint64_t)nrow);
-    if (k == 0) r = rs;
+    long r = nrow <= max_rows ? row0 + k : row0 + (long)(rng() % (uint64_t)nrow);
+    if (k == 0) r = row0;
     if (k == 1) r = re - 1;
     const double x = xt + (((double)r + 0.5) - yt) * dxdy;
-    const int got = rzb::cross_fast(e, (int)r, ncols);
+    const int got = rzb::cross_fast(e, (int)(r - row0), ncols);
     ++n_cross;
     if (got < 0) { ++n_fallback; continue; }
     if (std::isnan(x) || got != ref_boundary(x, ncols)) {
@@ -76,26 +80,40 @@ static double frac_bits(std::mt19937_64& rng, int mode) {
 int main() {
   std::mt19937_64 rng(20261204);
   // split_px against long double arithmetic
-  for (int i = 0; i < 3000000; ++i) {
+  for (int i = 0; i < 4000000; ++i) {
     double c;
     uint64_t b = rng();
-    switch (i % 3) {
+    switch (i % 4) {
       case 0: c = ((double)(int64_t)(b % 16000000) - 8000000.0) / 1.9; break;
       case 1: c = std::ldexp((double)(b >> 11), -(int)(b % 80)) * ((b & 1) ? -1 : 1); break;
-      default: c = std::nextafter(std::floor(((double)(b % 200000) - 100000.0)), (b & 2) ? 1e9 : -1e9); break;
+      case 2: c = std::nextafter(std::floor(((double)(b % 200000) - 100000.0)), (b & 2) ? 1e9 : -1e9); break;
+      default: {  // next to half pixels, where the first scanline changes
+        double h = std::floor((double)(b % 40000)) + 0.5;
+        for (int k = 0; k < (int)(b >> 60); ++k) h = std::nextafter(h, (b & 4) ? 1e9 : -1e9);
+        c = h;
+        break;
+      }
     }
-    int ci; float cf;
-    bool ok = rzb::split_px(c, ci, cf);
+    int ci; float cf; uint32_t f24 = 0;
+    bool ok = rzb::split_px(c, ci, cf, &f24);
     bool want_ok = std::fabs(c) < 4194304.0;
     if (ok != want_ok) { ++n_split_bad; continue; }
     if (!ok) continue;
     long double err = (long double)c - ((long double)ci + (long double)cf);
-    // ci is floor(c), or floor(c) + 1 when c lies within 2^-40 below an integer
+    // ci is floor(c), or floor(c) + 1 when c lies within 2^-24 below an integer
     const double fc = std::floor(c);
     if (!((double)ci == fc || (double)ci == fc + 1.0) || !(err > -0x1p-23L && err < 0x1p-23L) || cf < 0.0f ||
         cf > 1.0f) {
       if (n_split_bad < 5) printf("split %.17g -> %d %.9g\n", c, ci, cf);
       ++n_split_bad;
+      continue;
+    }
+    // the scanline of c from its split equals the exact helper's
+    for (int hi : {0, 7, 20000, 2147483646}) {
+      if (rzb::ceil_half_down_split(c, ok, ci, f24, hi) != rzb::ceil_half_down(c, hi)) {
+        if (n_split_bad < 5) printf("ceil_half_down_split %.17g hi=%d\n", c, hi);
+        ++n_split_bad;
+      }
     }
   }
   const double specials[] = {INFINITY, -INFINITY, NAN, 4194304.0, -4194304.0, 1e300, -0.0, 0.0, 5e-324};
