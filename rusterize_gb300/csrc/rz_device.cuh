@@ -92,6 +92,8 @@ struct Grid {
   int nrows, ncols;
   unsigned ntx;      // column tiles per row
   unsigned n_bands;
+  int touched;          // all_touched: lines and polygon rings take the AllTouched walk
+  unsigned poly_flags;  // flags of polygon fill records (DEDUP_BIT: the part's pixels are a set)
 };
 
 struct Geo {

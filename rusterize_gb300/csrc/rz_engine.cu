@@ -240,8 +240,6 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   if (tsize == 0) return fail(err, errlen, RZ_VALUE_ERROR, "Unsupported dtype");
   if ((int)fn < 0 || (int)fn > 6) return fail(err, errlen, RZ_VALUE_ERROR, "Unknown pixel function");
   if (band_of_geom && n_bands == 0) return fail(err, errlen, RZ_INVALID_ARGUMENT, "n_bands must be > 0");
-  if (flags & RZ_FLAG_ALL_TOUCHED)
-    return fail(err, errlen, RZ_VALUE_ERROR, "all_touched is not implemented by the GB300 engine yet");
   const bool in_dev = flags & RZ_FLAG_INPUT_DEVICE, out_dev = flags & RZ_FLAG_OUTPUT_DEVICE;
   const bool timing = !(flags & RZ_FLAG_NO_TIMING);
   const unsigned long long nb = band_of_geom ? n_bands : 1;
@@ -364,7 +362,12 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   // LineString::burn uses a PixelCache when pixels are not square
   // (burn_geometry.rs:179-185): writes of such a part are deduplicated.
   const bool line_dedup = info->xres != info->yres;
-  const bool dedup = line_dedup && (fn == RZ_SUM || fn == RZ_COUNT);
+  // all_touched: a part's pixels form a set (PixelCache for sum / count,
+  // prelude.rs:116-118; repeated writes of one value for the others)
+  const bool touched = (flags & RZ_FLAG_ALL_TOUCHED) != 0;
+  const bool dedup = (line_dedup || touched) && (fn == RZ_SUM || fn == RZ_COUNT);
+  gr.touched = touched ? 1 : 0;
+  gr.poly_flags = touched && dedup ? DEDUP_BIT : 0u;
 
   Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
   unsigned* part_geom = static_cast<unsigned*>(at(o_pg));
@@ -429,8 +432,9 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
                                                                                   d_ctrl);
       k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept, dedup ? DEDUP_BIT : 0u, sb,
                                            bcount, d_ctrl);
-      k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
-                                                               dedup ? DEDUP_BIT : 0u, sb, bcount, d_ctrl);
+      if (!touched)
+        k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
+                                                                 dedup ? DEDUP_BIT : 0u, sb, bcount, d_ctrl);
       k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, point_parts, sb, bcount, d_ctrl);
       launches += 5;
     }
@@ -569,8 +573,6 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   if (tsize == 0) return fail(err, errlen, RZ_VALUE_ERROR, "Unsupported dtype");
   if ((int)fn < 0 || (int)fn > 6) return fail(err, errlen, RZ_VALUE_ERROR, "Unknown pixel function");
   if (band_of_geom && n_bands == 0) return fail(err, errlen, RZ_INVALID_ARGUMENT, "n_bands must be > 0");
-  if (flags & RZ_FLAG_ALL_TOUCHED)
-    return fail(err, errlen, RZ_VALUE_ERROR, "all_touched is not implemented by the GB300 engine yet");
   const unsigned long long nb = band_of_geom ? n_bands : 1;
   if (info->nrows >= (1ull << 31) - 1 || info->ncols >= (1ull << 31) - 1)
     return fail(err, errlen, RZ_VALUE_ERROR, "raster dimensions must be below 2^31-1");
@@ -676,7 +678,11 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   gr.ncols = (int)ncols;
   gr.ntx = ntx;
   gr.n_bands = (unsigned)nb;
-  const bool dedup = info->xres != info->yres && (fn == RZ_SUM || fn == RZ_COUNT);
+  // PixelCache semantics as in rz_rasterize
+  const bool touched = (flags & RZ_FLAG_ALL_TOUCHED) != 0;
+  const bool dedup = (info->xres != info->yres || touched) && (fn == RZ_SUM || fn == RZ_COUNT);
+  gr.touched = touched ? 1 : 0;
+  gr.poly_flags = touched && dedup ? DEDUP_BIT : 0u;
 
   Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
   unsigned* part_geom = static_cast<unsigned*>(at(o_pg));
@@ -730,8 +736,9 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
     k_poly_spans<<<sms * nd.poly_bps, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, plan, poff, sb, bcount, d_ctrl);
     k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept, dedup ? DEDUP_BIT : 0u, sb,
                                          bcount, d_ctrl);
-    k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
-                                                             dedup ? DEDUP_BIT : 0u, sb, bcount, d_ctrl);
+    if (!touched)
+      k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
+                                                               dedup ? DEDUP_BIT : 0u, sb, bcount, d_ctrl);
     k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, point_parts, sb, bcount, d_ctrl);
     launches += 5;
   }

@@ -88,9 +88,11 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
       for (int o = 16; o > 0; o >>= 1) nonempty += __shfl_xor_sync(0xFFFFFFFFu, nonempty, o);
       edges += (lane == 0) ? (ve - vs) - nonempty : 0;
     }
-    if (kind == 1) {
+    if (kind == 1 || (kind == 2 && g.touched)) {  // all_touched also walks polygon rings
       c[PC_LINE_V] = ve - vs;
       c[PC_LINE_P] = 1;
+    }
+    if (kind == 1) {
     } else if (kind == 0) {
       c[PC_POINT_V] = ve - vs;
       c[PC_POINT_P] = 1;
@@ -180,7 +182,8 @@ __global__ void k_part_lists(Geo geo, const unsigned long long* off /*[P+1][PC_N
   for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < geo.n_parts;
        p += stride) {
     const unsigned kind = geo.part_kind[p];
-    if (kind == 1) line_parts[off[p * PC_N + PC_LINE_P]] = (unsigned)p;
+    if (kind == 1 || (kind == 2 && off[(p + 1) * PC_N + PC_LINE_P] > off[p * PC_N + PC_LINE_P]))
+      line_parts[off[p * PC_N + PC_LINE_P]] = (unsigned)p;
     else if (kind == 0) point_parts[off[p * PC_N + PC_POINT_P]] = (unsigned)p;
   }
 }
@@ -243,6 +246,92 @@ __device__ __forceinline__ void run_add(RunEmitter& re, const RecBuf& sb, unsign
   re.xb = x + 1;
 }
 
+// AllTouched::burn_line for one segment (burners.rs:94-247, adapted there
+// from GDAL's llrasterize.cpp): every pixel the segment touches, visited
+// left to right, calling emit(y, x) for those inside the raster.  The FP64
+// steps are the reference's, without FMA.  Returns false when the walk takes
+// more steps than a segment of its extent can need (pathological input),
+// after which the caller reports an error.
+template <typename Emit>
+__device__ __forceinline__ bool all_touched_walk(double df_x, double df_y, double df_x_end, double df_y_end,
+                                                 const Grid& g, Emit&& emit) {
+  const double EPSILON_INTERSECT = 1e-4, TOLERANCE = 1e-9;
+  const long long nrows = g.nrows, ncols = g.ncols;
+  const double nrows_f = (double)g.nrows, ncols_f = (double)g.ncols;
+  if (df_x > df_x_end) {  // proceed left to right
+    double t = df_x; df_x = df_x_end; df_x_end = t;
+    t = df_y; df_y = df_y_end; df_y_end = t;
+  }
+  if (fabs(__dsub_rn(df_x, df_x_end)) < 0.01) {  // vertical
+    if (df_y_end < df_y) { const double t = df_y; df_y = df_y_end; df_y_end = t; }
+    const long long ix = as_isize(floor(df_x_end));
+    long long iy = as_isize(floor(df_y));
+    long long iy_end = as_isize(floor(__dsub_rn(df_y_end, EPSILON_INTERSECT)));
+    if (ix < 0 || ix >= ncols) return true;
+    iy = iy > 0 ? iy : 0;
+    iy_end = iy_end < nrows - 1 ? iy_end : nrows - 1;
+    if (iy_end - iy > LINE_MAX_STEPS) return false;
+    for (long long y = iy; y <= iy_end; ++y) emit((int)y, (int)ix);
+    return true;
+  }
+  if (fabs(__dsub_rn(df_y, df_y_end)) < 0.01) {  // horizontal
+    if (df_x_end < df_x) { const double t = df_x; df_x = df_x_end; df_x_end = t; }
+    long long ix = as_isize(floor(df_x));
+    const long long iy = as_isize(floor(df_y));
+    long long ix_end = as_isize(floor(__dsub_rn(df_x_end, EPSILON_INTERSECT)));
+    if (iy < 0 || iy >= nrows) return true;
+    ix = ix > 0 ? ix : 0;
+    ix_end = ix_end < ncols - 1 ? ix_end : ncols - 1;
+    if (ix_end - ix > LINE_MAX_STEPS) return false;
+    for (long long x = ix; x <= ix_end; ++x) emit((int)iy, (int)x);
+    return true;
+  }
+  // sloped
+  const double slope = __ddiv_rn(__dsub_rn(df_y_end, df_y), __dsub_rn(df_x_end, df_x));
+  const double inv_slope = __ddiv_rn(1.0, slope);
+  if (df_x < 0.0) { df_y = __dadd_rn(df_y, __dmul_rn(__dsub_rn(0.0, df_x), slope)); df_x = 0.0; }
+  if (df_x_end > ncols_f) {
+    df_y_end = __dadd_rn(df_y_end, __dmul_rn(__dsub_rn(ncols_f, df_x_end), slope));
+    df_x_end = ncols_f;
+  }
+  if (df_y < 0.0) { df_x = __dadd_rn(df_x, __dmul_rn(__dsub_rn(0.0, df_y), inv_slope)); df_y = 0.0; }
+  else if (df_y > nrows_f) { df_x = __dadd_rn(df_x, __dmul_rn(__dsub_rn(nrows_f, df_y), inv_slope)); df_y = nrows_f; }
+  if (df_y_end < 0.0) df_x_end = __dadd_rn(df_x_end, __dmul_rn(__dsub_rn(0.0, df_y_end), inv_slope));
+  else if (df_y_end > nrows_f) df_x_end = __dadd_rn(df_x_end, __dmul_rn(__dsub_rn(nrows_f, df_y_end), inv_slope));
+  // clamp to the raster (f64::clamp)
+  df_x = df_x < 0.0 ? 0.0 : (df_x > ncols_f ? ncols_f : df_x);
+  df_x_end = df_x_end < 0.0 ? 0.0 : (df_x_end > ncols_f ? ncols_f : df_x_end);
+  // every step crosses a pixel boundary in x or y (or nudges y by TOLERANCE
+  // across one) and the clipped walk stays within the raster, so it needs
+  // fewer steps than this
+  long long budget = 4 * (ncols + nrows + 4) + 1024;
+  while (df_x >= 0.0 && df_x < df_x_end) {
+    if (--budget < 0) return false;
+    const long long ix = as_isize(floor(df_x));
+    const long long iy = as_isize(floor(df_y));
+    if (ix >= 0 && ix < ncols && iy >= 0 && iy < nrows) emit((int)iy, (int)ix);
+    double sx = __dsub_rn(floor(__dadd_rn(df_x, 1.0)), df_x);
+    double sy = __dmul_rn(sx, slope);
+    if (as_isize(floor(__dadd_rn(df_y, sy))) == iy) {
+      df_x = __dadd_rn(df_x, sx);
+      df_y = __dadd_rn(df_y, sy);
+    } else if (slope < 0.0) {
+      sy = __dsub_rn((double)iy, df_y);
+      if (sy > -TOLERANCE) sy = -TOLERANCE;
+      sx = __ddiv_rn(sy, slope);
+      df_x = __dadd_rn(df_x, sx);
+      df_y = __dadd_rn(df_y, sy);
+    } else {
+      sy = __dsub_rn((double)(iy + 1), df_y);
+      if (sy < TOLERANCE) sy = TOLERANCE;
+      sx = __ddiv_rn(sy, slope);
+      df_x = __dadd_rn(df_x, sx);
+      df_y = __dadd_rn(df_y, sy);
+    }
+  }
+  return true;
+}
+
 // One thread per line vertex v: segment (v, v+1) of its linestring, burned
 // with Standard::burn_line's integer Bresenham (burners.rs:40-91) after
 // extract_line's bbox filter (edges.rs:112-134).  The end pixel of the
@@ -272,6 +361,15 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
     const double min_x = min_rs(x0, x1), max_x = max_rs(x0, x1);
     const double min_y = min_rs(y0, y1), max_y = max_rs(y0, y1);
     if (!(min_x < (double)g.ncols && max_x >= 0.0 && min_y < (double)g.nrows && max_y >= 0.0)) continue;
+    const unsigned band = plan[p].band;
+    if (g.touched) {  // AllTouched::burn_line; polygon rings too (burn_geometry.rs:88-100, 226-238)
+      const bool ok = all_touched_walk(x0, y0, x1, y1, g, [&](int yy, int xx) {
+        run_add(run, sb, bucket_count, ctrl, g, band, p, dedup_flag, yy, xx);
+      });
+      run_flush(run, sb, bucket_count, ctrl, g, band, p, dedup_flag);
+      if (!ok) set_error(ctrl, ERR_LINE_LONG, v);
+      continue;
+    }
     atomicMax(&last_kept[p], v + 1);  // 0 = no kept segment
     long long ix0 = as_isize(floor(x0)), iy0 = as_isize(floor(y0));
     const long long ix1 = as_isize(floor(x1)), iy1 = as_isize(floor(y1));
@@ -286,7 +384,6 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
     const long long dy = -(iy1 > iy0 ? iy1 - iy0 : iy0 - iy1);
     const long long sx = ix0 < ix1 ? 1 : -1, sy = iy0 < iy1 ? 1 : -1;
     long long err = dx + dy;
-    const unsigned band = plan[p].band;
     while (ix0 != ix1 || iy0 != iy1) {
       if (ix0 >= 0 && ix0 < g.ncols && iy0 >= 0 && iy0 < g.nrows)
         run_add(run, sb, bucket_count, ctrl, g, band, p, dedup_flag, (int)iy0, (int)ix0);

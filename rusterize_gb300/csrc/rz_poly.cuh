@@ -384,7 +384,7 @@ __device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw,
     if (emit) {
       const int k = st_n + __popc(m & ((1u << lane) - 1u));
       ws.st_wid[k] = (band_wid + (unsigned)(r0 + row)) * wpr + w0 + (unsigned)wd;
-      ws.st_part[k] = part;
+      ws.st_part[k] = part | g.poly_flags;
       ws.st_mask[k] = cov;
       npix += (unsigned long long)__popc(cov);
     }
