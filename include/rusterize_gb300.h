@@ -192,6 +192,39 @@ rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void* values,
                        const rz_raster_info* info, rz_pixel_fn fn, rz_dtype out_dtype,
                        uint32_t flags, void* out, rz_stats* stats, char* err, size_t errlen);
 
+/* ---- sparse (COO) encoding ------------------------------------------- */
+
+typedef struct rz_sparse rz_sparse;
+
+/* Borrowed view of a sparse result (valid until rz_sparse_free): `count`
+ * (row, col, value) triplets, one per pixel write, grouped by band in band
+ * order (band_counts[b] triplets for band b), within a band by geometry in
+ * input order.  values are of `dtype`. */
+typedef struct {
+  uint64_t count;
+  uint32_t n_bands;
+  rz_dtype dtype;
+  const uint64_t* band_counts; /* [n_bands] */
+  const uint64_t* rows;        /* [count] */
+  const uint64_t* cols;        /* [count] */
+  const void* values;          /* [count] */
+} rz_sparse_view;
+
+/* Replaces SparseArray's ArrayBuilder::build (rust/src/rasterize.rs:118-152)
+ * with the SparseArrayWriter it fills (rust/src/encoding/writers.rs:86-131):
+ * the pixel writes of every geometry as COO triplets instead of a dense
+ * raster.  Arguments as rz_rasterize (no background, host output only); the
+ * pixel function only decides the PixelCache deduplication of all_touched
+ * (prelude.rs:116-118).  The multiset of triplets of each geometry and the
+ * order of the geometries are the reference's; within one geometry the
+ * triplets come row by row, left to right. */
+rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, const void* values,
+                              const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
+                              rz_pixel_fn fn, rz_dtype out_dtype, uint32_t flags, rz_sparse** out,
+                              rz_stats* stats, char* err, size_t errlen);
+rz_status rz_sparse_view_get(const rz_sparse* sp, rz_sparse_view* out);
+void rz_sparse_free(rz_sparse* sp);
+
 /* The context's CUDA stream (a cudaStream_t), e.g. to record CUDA events
  * around calls or to order other work after them. */
 void* rz_context_stream(rz_context* ctx);

@@ -49,6 +49,13 @@ def load():
         lib.rzo_raster_info.restype = c_int
         lib.rzo_raster_info.argtypes = [c_uint64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                         c_uint32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+        lib.rzo_rasterize_sparse.restype = c_int
+        lib.rzo_rasterize_sparse.argtypes = [c_uint64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                             c_int, c_void_p, c_uint32, c_void_p, c_uint64, c_uint64, c_int, c_int,
+                                             POINTER(c_uint64), POINTER(c_void_p), POINTER(c_void_p),
+                                             POINTER(c_void_p), c_void_p]
+        lib.rzo_free.restype = None
+        lib.rzo_free.argtypes = [c_void_p]
         _lib = lib
     return _lib
 
@@ -115,3 +122,46 @@ def rasterize(table, nrows, ncols, xmin, xmax, ymin, ymax, xres, yres, *, values
         counters["pixel_writes"] = nw.value
         counters["edges"] = ne.value
     return out
+
+
+def rasterize_sparse(table, nrows, ncols, xmin, xmax, ymin, ymax, xres, yres, *, values=None, fn="last",
+                     dtype="float64", bands=None, n_bands=None, all_touched=False):
+    """Sparse burn with the CPU restatement: (band_counts, rows, cols, values)
+    in the reference's write order (SparseArrayWriter, writers.rs:86-131)."""
+    lib = load()
+    po, pk, ro, vo, rf, xy = _arrays(table)
+    dt = np.dtype(dtype)
+    G = len(po) - 1
+    if values is None:
+        vals = None
+    elif np.isscalar(values) or (isinstance(values, np.ndarray) and values.ndim == 0):
+        vals = np.full(G, values, dtype=dt)
+    else:
+        vals = np.ascontiguousarray(values, dtype=dt)
+    if bands is not None:
+        bands = np.ascontiguousarray(bands, np.uint32)
+        nb = int(n_bands if n_bands is not None else (bands.max() + 1 if len(bands) else 1))
+    else:
+        nb = 1
+    raster = np.array([xmin, xmax, ymin, ymax, xres, yres], np.float64)
+    count = c_uint64(0)
+    rows_p, cols_p, vals_p = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    band_counts = np.zeros(nb, np.uint64)
+    st = lib.rzo_rasterize_sparse(G, po.ctypes.data, pk.ctypes.data, ro.ctypes.data, vo.ctypes.data, xy.ctypes.data,
+                                  None if vals is None else vals.ctypes.data, DTYPES[dt.name],
+                                  None if bands is None else bands.ctypes.data, nb, raster.ctypes.data, nrows, ncols,
+                                  PIXEL_FNS[fn], int(bool(all_touched)), ctypes.byref(count), ctypes.byref(rows_p),
+                                  ctypes.byref(cols_p), ctypes.byref(vals_p), band_counts.ctypes.data)
+    if st:
+        raise ValueError(f"oracle failed with status {st}")
+    n = count.value
+    try:
+        rows = np.ctypeslib.as_array(ctypes.cast(rows_p, ctypes.POINTER(ctypes.c_uint64)), (max(n, 1),))[:n].copy()
+        cols = np.ctypeslib.as_array(ctypes.cast(cols_p, ctypes.POINTER(ctypes.c_uint64)), (max(n, 1),))[:n].copy()
+        raw = ctypes.string_at(vals_p, n * dt.itemsize) if n else b""
+        out_vals = np.frombuffer(raw, dtype=dt).copy()
+    finally:
+        for p_ in (rows_p, cols_p, vals_p):
+            lib.rzo_free(p_)
+    return band_counts, rows, cols, out_vals
+

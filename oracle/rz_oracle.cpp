@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <cstdlib>
 #include <limits>
 #include <vector>
 
@@ -256,11 +257,21 @@ struct Writer {
   PixelCache* cache = nullptr;
   int mode = 0;  // 0 direct, 1 LineWriter, 2 FillWriter
   uint64_t* nwrites = nullptr;
+  // SparseArrayWriter (writers.rs:86-131): record the triplet instead
+  std::vector<uint64_t>* srows = nullptr;
+  std::vector<uint64_t>* scols = nullptr;
+  std::vector<T>* svals = nullptr;
 
   void write(uint64_t y, uint64_t x, T value) {
     if (mode == 1) { if (!cache->insert(x, y)) return; }
     else if (mode == 2) { if (cache->contains(x, y)) return; }
     if (nwrites) ++*nwrites;
+    if (srows) {
+      srows->push_back(y);
+      scols->push_back(x);
+      svals->push_back(value);
+      return;
+    }
     apply_fn(fn, band[y * ncols + x], value, bg);
   }
 };
@@ -488,6 +499,40 @@ int rasterize_t(const Geoms& g, const T* values, const uint32_t* band_of_geom, u
   return 0;
 }
 
+// SparseArray::build (rasterize.rs:118-152): per band (in band order) the
+// triplets of its geometries in index order; bands concatenated.
+template <typename T>
+int rasterize_sparse_t(const Geoms& g, const T* values, const uint32_t* band_of_geom, uint32_t n_bands,
+                       const RasterInfo& ri, int fn, bool all_touched, std::vector<uint64_t>& rows,
+                       std::vector<uint64_t>& cols, std::vector<T>& vals, uint64_t* band_counts) {
+  uint64_t nb = band_of_geom ? n_bands : 1;
+  bool dedup = all_touched && (fn == FN_SUM || fn == FN_COUNT);
+  std::vector<std::vector<uint64_t>> br(nb), bc(nb);
+  std::vector<std::vector<T>> bv(nb);
+  for (uint64_t i = 0; i < g.n_geoms; ++i) {
+    uint64_t b = band_of_geom ? band_of_geom[i] : 0;
+    if (b >= nb) return -1;
+    Writer<T> w;
+    w.band = nullptr;
+    w.ncols = ri.ncols;
+    w.fn = fn;
+    w.bg = (T)0;
+    w.srows = &br[b];
+    w.scols = &bc[b];
+    w.svals = &bv[b];
+    T v = values ? values[i] : (T)1;
+    for (uint64_t p = g.part_offsets[i]; p < g.part_offsets[i + 1]; ++p)
+      burn_part<T>(g, p, ri, v, w, all_touched, dedup, nullptr);
+  }
+  for (uint64_t b = 0; b < nb; ++b) {
+    band_counts[b] = br[b].size();
+    rows.insert(rows.end(), br[b].begin(), br[b].end());
+    cols.insert(cols.end(), bc[b].begin(), bc[b].end());
+    vals.insert(vals.end(), bv[b].begin(), bv[b].end());
+  }
+  return 0;
+}
+
 // --------------------------------------------------------- raster info ----
 // geo BoundingRect as used by RasterInfoBuilder::build_with (raster.rs:75-86):
 // points/lines use every coordinate, polygons only exterior rings.
@@ -533,6 +578,63 @@ int rzo_rasterize(uint64_t n_geoms, const uint64_t* part_offsets, const uint8_t*
   }
 #undef RZO_CASE
 }
+
+// Sparse (COO) burn: triplets in the reference's write order, in buffers
+// allocated with malloc (free them with rzo_free).  band_counts has n_bands
+// entries (1 without bands).
+int rzo_rasterize_sparse(uint64_t n_geoms, const uint64_t* part_offsets, const uint8_t* part_kind,
+                         const uint64_t* ring_offsets, const uint64_t* vertex_offsets, const double* xy,
+                         const void* values, int dtype, const uint32_t* band_of_geom, uint32_t n_bands,
+                         const double* raster, uint64_t nrows, uint64_t ncols, int pixel_fn, int all_touched,
+                         uint64_t* count, uint64_t** rows_out, uint64_t** cols_out, void** vals_out,
+                         uint64_t* band_counts) {
+  Geoms g{n_geoms, part_offsets, part_kind, ring_offsets, vertex_offsets, nullptr, xy};
+  RasterInfo ri{ncols, nrows, raster[0], raster[1], raster[2], raster[3], raster[4], raster[5]};
+  bool at = all_touched != 0;
+  std::vector<uint64_t> rows, cols;
+  int st = -2;
+  size_t tsize = 0;
+  void* vbuf = nullptr;
+#define RZO_SCASE(CODE, T)                                                                                 \
+  case CODE: {                                                                                             \
+    std::vector<T> vals;                                                                                   \
+    st = rasterize_sparse_t<T>(g, (const T*)values, band_of_geom, n_bands, ri, pixel_fn, at, rows, cols,  \
+                               vals, band_counts);                                                         \
+    tsize = sizeof(T);                                                                                     \
+    vbuf = std::malloc(vals.size() * tsize + 1);                                                           \
+    if (vbuf && !vals.empty()) std::memcpy(vbuf, vals.data(), vals.size() * tsize);                       \
+    break;                                                                                                 \
+  }
+  switch (dtype) {
+    RZO_SCASE(DT_U8, uint8_t)
+    RZO_SCASE(DT_U16, uint16_t)
+    RZO_SCASE(DT_U32, uint32_t)
+    RZO_SCASE(DT_U64, uint64_t)
+    RZO_SCASE(DT_I8, int8_t)
+    RZO_SCASE(DT_I16, int16_t)
+    RZO_SCASE(DT_I32, int32_t)
+    RZO_SCASE(DT_I64, int64_t)
+    RZO_SCASE(DT_F32, float)
+    RZO_SCASE(DT_F64, double)
+    default: return -2;
+  }
+#undef RZO_SCASE
+  if (st != 0) {
+    std::free(vbuf);
+    return st;
+  }
+  *count = rows.size();
+  *rows_out = (uint64_t*)std::malloc(rows.size() * 8 + 8);
+  *cols_out = (uint64_t*)std::malloc(cols.size() * 8 + 8);
+  if (!rows.empty()) {
+    std::memcpy(*rows_out, rows.data(), rows.size() * 8);
+    std::memcpy(*cols_out, cols.data(), cols.size() * 8);
+  }
+  *vals_out = vbuf;
+  return 0;
+}
+
+void rzo_free(void* p) { std::free(p); }
 
 // Restatement of RasterInfoBuilder (rust/src/geo/raster.rs:50-156) as driven
 // by RawRasterInfo::build (python/src/geo/raster.rs:17-41).

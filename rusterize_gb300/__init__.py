@@ -25,14 +25,15 @@ from ._dependencies import polars as pl
 from ._dependencies import xarray as xr
 from ._lib import Context, EngineError, NoDeviceError, PanicException, default_context
 from ._native import _rusterize, group_keys, parse_geometry
-from .engine import RasterInfo, raster_info, rasterize_table
+from .engine import RasterInfo, raster_info, rasterize_table, rasterize_table_sparse
 from .geometry import GeometryTable, TableBuilder, from_wkb, from_wkt
+from .sparse import SparseArray
 
 __version__ = "0.1.0"
 
 __all__ = [
     "rusterize", "_rusterize", "GeometryTable", "TableBuilder", "from_wkt", "from_wkb", "RasterInfo",
-    "raster_info", "rasterize_table", "group_keys", "parse_geometry", "Context", "default_context",
+    "raster_info", "rasterize_table", "rasterize_table_sparse", "SparseArray", "group_keys", "parse_geometry", "Context", "default_context",
     "PanicException", "EngineError", "NoDeviceError",
 ]
 

@@ -82,6 +82,13 @@ class RzStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class RzSparseView(ctypes.Structure):
+    _fields_ = [
+        ("count", c_uint64), ("n_bands", c_uint32), ("dtype", c_int),
+        ("band_counts", c_void_p), ("rows", c_void_p), ("cols", c_void_p), ("values", c_void_p),
+    ]
+
+
 # exported symbols and their prototypes (restype, argtypes)
 PROTOTYPES = {
     "rz_abi_version": (c_int, []),
@@ -105,6 +112,10 @@ PROTOTYPES = {
     "rz_rasterize_noalloc": (c_int, [c_void_p, POINTER(RzGeoms), c_void_p, c_void_p, c_void_p, c_uint32,
                                      POINTER(RzRasterInfo), c_int, c_int, c_uint32, c_void_p, POINTER(RzStats),
                                      c_char_p, c_size_t]),
+    "rz_rasterize_sparse": (c_int, [c_void_p, POINTER(RzGeoms), c_void_p, c_void_p, c_uint32, POINTER(RzRasterInfo),
+                                    c_int, c_int, c_uint32, POINTER(c_void_p), POINTER(RzStats), c_char_p, c_size_t]),
+    "rz_sparse_view_get": (c_int, [c_void_p, POINTER(RzSparseView)]),
+    "rz_sparse_free": (None, [c_void_p]),
 }
 
 _lib = None

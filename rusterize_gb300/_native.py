@@ -16,8 +16,9 @@ import numpy as np
 from . import _lib
 from ._dependencies import SHAPELY_AVAILABLE, shapely
 from ._lib import PanicException
-from .engine import RasterInfo, raster_info, rasterize_table
+from .engine import RasterInfo, raster_info, rasterize_table, rasterize_table_sparse
 from .geometry import GeometryTable, from_wkb, from_wkt
+from .sparse import SparseArray, _Burn
 
 
 def parse_geometry(obj: Any) -> GeometryTable:
@@ -116,8 +117,6 @@ def _rusterize(geometry: Any, raw_raster_info: dict, pypixel_fn: str, pydf: Any 
         raise ValueError("Unknown pixel function")
     if pydtype not in _lib.DTYPES or pyencoding not in ("xarray", "numpy", "sparse"):
         raise PanicException("not implemented: Invalid dtype or encoding provided.")
-    if pyencoding == "sparse":
-        raise NotImplementedError("encoding='sparse' is not implemented by the GB300 engine yet")
     dt = np.dtype(pydtype)
 
     # rusterize.rs:50-53: background.extract::<T>().ok().unwrap_or_default()
@@ -173,6 +172,13 @@ def _rusterize(geometry: Any, raw_raster_info: dict, pypixel_fn: str, pydf: Any 
         if bands is not None:
             bands = bands[idx]
 
+    if pyencoding == "sparse":  # rusterize.rs:166-176 -> SparseArray (arrays.rs:62-101)
+        band_counts, rows, cols, vals = rasterize_table_sparse(
+            table, info, values=values, fn=pypixel_fn, dtype=pydtype, bands=bands, n_bands=len(band_names),
+            all_touched=bool(pytouched), context=context, stats=stats)
+        burn = _Burn(table=table, values=values, fn=pypixel_fn, dtype=pydtype, background=bg, bands=bands,
+                     all_touched=bool(pytouched))
+        return SparseArray(band_names, band_counts, rows, cols, vals, info, burn)
     out = rasterize_table(table, info, values=values, fn=pypixel_fn, background=bg, dtype=pydtype, bands=bands,
                           n_bands=len(band_names), all_touched=bool(pytouched), context=context, stats=stats)
     if pyencoding == "xarray":

@@ -17,6 +17,8 @@
 #include "rz_internal.h"
 #include "rz_kernels.cuh"
 #include "rz_scan.cuh"
+#include "rz_sort.cuh"
+#include "rz_sparse.cuh"
 
 using rz::fail;
 using namespace rzd;
@@ -108,13 +110,21 @@ unsigned grid_for(unsigned long long work, unsigned per_block, unsigned cap) {
 
 }  // namespace
 
+// Host copy of a sparse (COO) result.
+struct rz_sparse {
+  std::vector<uint64_t> band_counts, rows, cols;
+  std::vector<unsigned char> values;
+  uint32_t n_bands = 1;
+  rz_dtype dtype = RZ_F64;
+};
+
 struct rz_context {
   int device = 0;
   int num_sms = 0;
   int poly_blocks_per_sm = 1;
   int narrow_blocks_per_sm = 1;
   cudaStream_t stream = nullptr;
-  DevBuf main, spans, out;
+  DevBuf main, spans, out, sparse;
   cudaEvent_t ev[8] = {};
   Ctrl* h_ctrl = nullptr;  // pinned
   unsigned long long span_cap_hint = 0;
@@ -184,7 +194,7 @@ extern "C" void rz_context_destroy(rz_context* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out})
+  for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out, &ctx->sparse})
     if (b->p) cudaFree(b->p);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
@@ -197,7 +207,7 @@ extern "C" rz_status rz_context_trim(rz_context* ctx) {
   if (!ctx) return RZ_INVALID_ARGUMENT;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out}) {
+  for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out, &ctx->sparse}) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
     b->cap = 0;
@@ -226,15 +236,18 @@ __global__ void k_reset_pass(Ctrl* c) {
   c->fill_work = 0;
 }
 
-extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void* values, const void* background,
-                                  const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
-                                  rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats,
-                                  char* err, size_t errlen) {
+// The burn pipeline shared by the dense and the sparse entry points; with
+// `sp` the coverage records are turned into COO triplets instead of being
+// scattered into buckets and filled.
+static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* values, const void* background,
+                           const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
+                           rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats, char* err,
+                           size_t errlen, rz_sparse* sp) {
   using clk = std::chrono::steady_clock;
   const auto t_host0 = clk::now();
   rz::clear_err(err, errlen);
   if (stats) std::memset(stats, 0, sizeof(*stats));
-  if (!ctx || !g || !info || !background || !out)
+  if (!ctx || !g || !info || (!sp && (!background || !out)))
     return fail(err, errlen, RZ_INVALID_ARGUMENT, "null argument");
   const size_t tsize = rz_dtype_size(dt);
   if (tsize == 0) return fail(err, errlen, RZ_VALUE_ERROR, "Unsupported dtype");
@@ -264,13 +277,18 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
       return fail(err, errlen, RZ_INVALID_ARGUMENT, "geometry table sizes are inconsistent");
   }
   unsigned long long bg_bits = 0, scalar_bits = one_bits(dt);
-  std::memcpy(&bg_bits, background, tsize);
+  if (background) std::memcpy(&bg_bits, background, tsize);
   const bool per_geom_values = values && !(flags & RZ_FLAG_SCALAR_VALUE);
   if (values && (flags & RZ_FLAG_SCALAR_VALUE)) {
     scalar_bits = 0;
     std::memcpy(&scalar_bits, values, tsize);
   }
   if (stats) stats->out_bytes = out_elems * tsize;
+  if (sp) {
+    sp->n_bands = (uint32_t)nb;
+    sp->dtype = dt;
+    sp->band_counts.assign(nb, 0);
+  }
   if (out_elems == 0) return RZ_OK;
 
   RZ_CUDA(cudaSetDevice(ctx->device));
@@ -302,7 +320,7 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   const size_t o_big = L.take(4 * nbuckets);
   const size_t o_ctrl = L.take(sizeof(Ctrl));
   RZ_CUDA(ensure(ctx->main, L.off));
-  if (!out_dev) RZ_CUDA(ensure(ctx->out, out_elems * tsize));
+  if (!out_dev && !sp) RZ_CUDA(ensure(ctx->out, out_elems * tsize));
   unsigned long long cap = std::max<unsigned long long>(ctx->span_cap_hint, 2 * V + (1ull << 20));
   if (cap > 0xFFFFFFF0ull) cap = 0xFFFFFFF0ull;
   RZ_CUDA(ensure(ctx->spans, RECORD_BYTES * cap + 16));
@@ -368,6 +386,10 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   const bool dedup = (line_dedup || touched) && (fn == RZ_SUM || fn == RZ_COUNT);
   gr.touched = touched ? 1 : 0;
   gr.poly_flags = touched && dedup ? DEDUP_BIT : 0u;
+  // lines: a dense raster only needs the PixelCache where a repeated write
+  // changes the pixel (sum / count); the triplet stream of the sparse
+  // encoding drops every repeat the cache drops (burn_geometry.rs:179-185)
+  const unsigned line_flag = (dedup || (sp && line_dedup)) ? DEDUP_BIT : 0u;
 
   Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
   unsigned* part_geom = static_cast<unsigned*>(at(o_pg));
@@ -430,15 +452,16 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
           geo, gr, plan, poff, sb, bcount, d_ctrl);
       k_poly_spans<<<sms * ctx->poly_blocks_per_sm, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, plan, poff, sb, bcount,
                                                                                   d_ctrl);
-      k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept, dedup ? DEDUP_BIT : 0u, sb,
+      k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept, line_flag, sb,
                                            bcount, d_ctrl);
       if (!touched)
         k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
-                                                                 dedup ? DEDUP_BIT : 0u, sb, bcount, d_ctrl);
+                                                                 line_flag, sb, bcount, d_ctrl);
       k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, point_parts, sb, bcount, d_ctrl);
       launches += 5;
     }
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[3], s));
+    if (!sp) {
     launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
     launch_scatter(tsize, sms, s, sb, boff, bcount, sorted, d_values, part_geom, rvals, d_ctrl);
     ++launches;
@@ -463,8 +486,12 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     fa.ctrl = d_ctrl;
     fa.rec_cap = cap;
     launches += fill(fa, (int)fn, dedup, sms, s);
+    }
     RZ_CUDA(cudaGetLastError());
-    if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[5], s));
+    if (timing) {
+      if (sp) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
+      RZ_CUDA(cudaEventRecord(ctx->ev[5], s));
+    }
     RZ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
     RZ_CUDA(cudaStreamSynchronize(s));
     const Ctrl& hc = *ctx->h_ctrl;
@@ -509,7 +536,113 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
     }
     break;
   }
-  if (!out_dev) {
+  if (sp) {
+    // ---- sparse: order the records by (band, part, row, word), expand ----
+    const unsigned long long n = ctx->h_ctrl->span_count;
+    RecBuf sbr;
+    sbr.cap = cap;
+    sbr.wid = static_cast<unsigned*>(ctx->spans.p);
+    sbr.part = sbr.wid + cap;
+    sbr.mask = sbr.part + cap;
+    const unsigned wpr = ntx * WPT;
+    const unsigned long long nsort = std::max<unsigned long long>(n, nb > 1 ? P : 0);
+    Layout SL;
+    const size_t o_k0 = SL.take(8 * (nsort ? nsort : 1)), o_k1 = SL.take(8 * (nsort ? nsort : 1));
+    const size_t o_v0 = SL.take(4 * (nsort ? nsort : 1)), o_v1 = SL.take(4 * (nsort ? nsort : 1));
+    const size_t o_pr = SL.take(4 * (P ? P : 1));
+    const size_t o_eff = SL.take(4 * (n ? n : 1));
+    const size_t o_cnt2 = SL.take(8 * (n + 1));
+    const size_t o_off2 = SL.take(8 * (n + 1));
+    const size_t o_st64 = SL.take(8 * scan_temp_elems(n ? n : 1, 1));
+    const size_t o_rst = SL.take(4 * radix_sort_temp_words(nsort ? nsort : 1));
+    const size_t o_bc = SL.take(8 * nb);
+    const size_t base_bytes = SL.off;
+    RZ_CUDA(ensure(ctx->sparse, base_bytes));
+    char* sbase = static_cast<char*>(ctx->sparse.p);
+    auto sat = [&](size_t o) { return static_cast<void*>(sbase + o); };
+    unsigned long long* k0 = static_cast<unsigned long long*>(sat(o_k0));
+    unsigned long long* k1 = static_cast<unsigned long long*>(sat(o_k1));
+    unsigned* v0 = static_cast<unsigned*>(sat(o_v0));
+    unsigned* v1 = static_cast<unsigned*>(sat(o_v1));
+    unsigned* prank = nullptr;
+    int bits_part = 1;
+    while ((1ull << bits_part) < P) ++bits_part;
+    if (nb > 1 && P) {  // band-major rank of every part
+      k_part_band_keys<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(plan, P, k0, v0);
+      int bits_band = 1;
+      while ((1ull << bits_band) < nb) ++bits_band;
+      const bool in_tmp = radix_sort(k0, v0, k1, v1, (unsigned)P, 32 + bits_band,
+                                     static_cast<unsigned*>(sat(o_rst)), s, launches);
+      prank = static_cast<unsigned*>(sat(o_pr));
+      k_part_rank<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(in_tmp ? v1 : v0, P, prank);
+      launches += 2;
+    }
+    unsigned long long* skeys = k0;
+    unsigned* svals = v0;
+    unsigned long long total = 0;
+    unsigned long long* bcnt = static_cast<unsigned long long*>(sat(o_bc));
+    RZ_CUDA(cudaMemsetAsync(bcnt, 0, 8 * nb, s));
+    if (n) {
+      k_rec_keys<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(sbr, n, prank, plan, (unsigned)(nrows * wpr), k0, v0);
+      const bool in_tmp = radix_sort(k0, v0, k1, v1, (unsigned)n, 32 + bits_part,
+                                     static_cast<unsigned*>(sat(o_rst)), s, launches);
+      skeys = in_tmp ? k1 : k0;
+      svals = in_tmp ? v1 : v0;
+      unsigned* eff = static_cast<unsigned*>(sat(o_eff));
+      unsigned long long* cnt = static_cast<unsigned long long*>(sat(o_cnt2));
+      unsigned long long* off = static_cast<unsigned long long*>(sat(o_off2));
+      k_sparse_count<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(skeys, svals, n, sbr, eff, cnt);
+      launches += 2 + scan<unsigned long long, 1>(cnt, off, n, static_cast<unsigned long long*>(sat(o_st64)), s);
+      RZ_CUDA(cudaMemcpyAsync(&total, off + n, 8, cudaMemcpyDeviceToHost, s));
+      RZ_CUDA(cudaStreamSynchronize(s));
+      sp->rows.resize(total);
+      sp->cols.resize(total);
+      sp->values.resize(total * tsize);
+      if (total) {
+        // the triplet arrays go after the sort scratch (grow-only buffer)
+        const size_t o_rows = (base_bytes + 255) & ~size_t(255);
+        const size_t o_cols = o_rows + ((8 * total + 255) & ~size_t(255));
+        const size_t o_vals = o_cols + ((8 * total + 255) & ~size_t(255));
+        const size_t need = o_vals + tsize * total;
+        if (need > ctx->sparse.cap) {
+          // keep the ordered records: copy the live part of the scratch
+          DevBuf grown;
+          RZ_CUDA(ensure(grown, need));
+          RZ_CUDA(cudaMemcpyAsync(grown.p, ctx->sparse.p, base_bytes, cudaMemcpyDeviceToDevice, s));
+          RZ_CUDA(cudaStreamSynchronize(s));
+          cudaFree(ctx->sparse.p);
+          ctx->sparse = grown;
+          sbase = static_cast<char*>(ctx->sparse.p);
+          skeys = static_cast<unsigned long long*>(sat(in_tmp ? o_k1 : o_k0));
+          svals = static_cast<unsigned*>(sat(in_tmp ? o_v1 : o_v0));
+          eff = static_cast<unsigned*>(sat(o_eff));
+          off = static_cast<unsigned long long*>(sat(o_off2));
+          bcnt = static_cast<unsigned long long*>(sat(o_bc));
+        }
+        unsigned long long* trows = static_cast<unsigned long long*>(sat(o_rows));
+        unsigned long long* tcols = static_cast<unsigned long long*>(sat(o_cols));
+        void* tvals = sat(o_vals);
+        const unsigned eg = grid_for(n, 256, sms * 16);
+        switch (tsize) {
+          case 1: k_sparse_emit<1><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, wpr, d_values, part_geom,
+                                                      scalar_bits, trows, tcols, tvals, bcnt); break;
+          case 2: k_sparse_emit<2><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, wpr, d_values, part_geom,
+                                                      scalar_bits, trows, tcols, tvals, bcnt); break;
+          case 4: k_sparse_emit<4><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, wpr, d_values, part_geom,
+                                                      scalar_bits, trows, tcols, tvals, bcnt); break;
+          default: k_sparse_emit<8><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, wpr, d_values,
+                                                       part_geom, scalar_bits, trows, tcols, tvals, bcnt); break;
+        }
+        ++launches;
+        RZ_CUDA(cudaGetLastError());
+        RZ_CUDA(cudaMemcpyAsync(sp->rows.data(), trows, 8 * total, cudaMemcpyDeviceToHost, s));
+        RZ_CUDA(cudaMemcpyAsync(sp->cols.data(), tcols, 8 * total, cudaMemcpyDeviceToHost, s));
+        RZ_CUDA(cudaMemcpyAsync(sp->values.data(), tvals, tsize * total, cudaMemcpyDeviceToHost, s));
+      }
+    }
+    RZ_CUDA(cudaMemcpyAsync(sp->band_counts.data(), bcnt, 8 * nb, cudaMemcpyDeviceToHost, s));
+    if (stats) stats->pixel_writes = total;
+  } else if (!out_dev) {
     RZ_CUDA(cudaMemcpyAsync(out, d_out, out_elems * tsize, cudaMemcpyDeviceToHost, s));
   }
   if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[6], s));
@@ -532,6 +665,48 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
   }
   return RZ_OK;
 }
+
+extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void* values, const void* background,
+                                  const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
+                                  rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats,
+                                  char* err, size_t errlen) {
+  return burn_impl(ctx, g, values, background, band_of_geom, n_bands, info, fn, dt, flags, out, stats, err, errlen,
+                   nullptr);
+}
+
+extern "C" rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, const void* values,
+                                         const uint32_t* band_of_geom, uint32_t n_bands,
+                                         const rz_raster_info* info, rz_pixel_fn fn, rz_dtype dt, uint32_t flags,
+                                         rz_sparse** out, rz_stats* stats, char* err, size_t errlen) {
+  rz::clear_err(err, errlen);
+  if (!out) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (flags & RZ_FLAG_OUTPUT_DEVICE)
+    return fail(err, errlen, RZ_INVALID_ARGUMENT, "the sparse encoding returns host arrays");
+  auto* sp = new rz_sparse();
+  const rz_status st = burn_impl(ctx, g, values, nullptr, band_of_geom, n_bands, info, fn, dt, flags, nullptr, stats,
+                                 err, errlen, sp);
+  if (st != RZ_OK) {
+    delete sp;
+    return st;
+  }
+  *out = sp;
+  return RZ_OK;
+}
+
+extern "C" rz_status rz_sparse_view_get(const rz_sparse* sp, rz_sparse_view* out) {
+  if (!sp || !out) return RZ_INVALID_ARGUMENT;
+  out->count = sp->rows.size();
+  out->n_bands = sp->n_bands;
+  out->dtype = sp->dtype;
+  out->band_counts = sp->band_counts.data();
+  out->rows = sp->rows.data();
+  out->cols = sp->cols.data();
+  out->values = sp->values.data();
+  return RZ_OK;
+}
+
+extern "C" void rz_sparse_free(rz_sparse* sp) { delete sp; }
 
 // ---------------------------------------------------------------------------
 // Allocation-free burn (rz_rasterize_noalloc).

@@ -363,10 +363,13 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
     if (!(min_x < (double)g.ncols && max_x >= 0.0 && min_y < (double)g.nrows && max_y >= 0.0)) continue;
     const unsigned band = plan[p].band;
     if (g.touched) {  // AllTouched::burn_line; polygon rings too (burn_geometry.rs:88-100, 226-238)
+      // a polygon's ring walk shares the polygon's PixelCache (sum / count
+      // only); the non-square-pixel cache of LineString::burn is not its
+      const unsigned flag = geo.part_kind[p] == 2 ? g.poly_flags : dedup_flag;
       const bool ok = all_touched_walk(x0, y0, x1, y1, g, [&](int yy, int xx) {
-        run_add(run, sb, bucket_count, ctrl, g, band, p, dedup_flag, yy, xx);
+        run_add(run, sb, bucket_count, ctrl, g, band, p, flag, yy, xx);
       });
-      run_flush(run, sb, bucket_count, ctrl, g, band, p, dedup_flag);
+      run_flush(run, sb, bucket_count, ctrl, g, band, p, flag);
       if (!ok) set_error(ctrl, ERR_LINE_LONG, v);
       continue;
     }

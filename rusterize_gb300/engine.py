@@ -123,3 +123,67 @@ def rasterize_table(table: GeometryTable, info: RasterInfo, *, values=None, fn: 
     if stats is not None:
         stats.update(st_c.as_dict())
     return out
+
+
+def rasterize_table_sparse(table: GeometryTable, info: RasterInfo, *, values=None, fn: str = "last",
+                           dtype: str = "float64", bands: np.ndarray | None = None, n_bands: int | None = None,
+                           all_touched: bool = False, context: _lib.Context | None = None,
+                           stats: dict | None = None) -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+    """Burn ``table`` as COO triplets (the SparseArrayWriter stream,
+    rust/src/encoding/writers.rs:86-131): returns (band_counts, rows, cols,
+    values) with the triplets grouped by band in band order."""
+    lib = _lib.load()
+    if dtype not in _lib.DTYPES:
+        raise ValueError(f"Unsupported dtype {dtype!r}")
+    if fn not in _lib.PIXEL_FNS:
+        raise ValueError("Unknown pixel function")
+    np_dt = np.dtype(dtype)
+    ctx = context or _lib.default_context()
+    nb = 1
+    c_bands = None
+    if bands is not None:
+        bands = np.ascontiguousarray(bands, dtype=np.uint32)
+        nb = int(n_bands if n_bands is not None else (int(bands.max()) + 1 if len(bands) else 1))
+        c_bands = bands.ctypes.data
+    flags = _lib.FLAG_ALL_TOUCHED if all_touched else 0
+    vals_arr = None
+    c_vals = None
+    if values is not None:
+        if np.isscalar(values) or (isinstance(values, np.ndarray) and values.ndim == 0):
+            vals_arr = np.array([values], dtype=np_dt)
+            flags |= _lib.FLAG_SCALAR_VALUE
+        else:
+            vals_arr = np.ascontiguousarray(values, dtype=np_dt)
+            if len(vals_arr) != table.n_geoms:
+                raise ValueError("Geometry and field lengths must match")
+        c_vals = vals_arr.ctypes.data
+    g = table.c_view()
+    ri = info.c_struct()
+    st_c = _lib.RzStats()
+    e = _lib.errbuf()
+    h = ctypes.c_void_p()
+    with ctx.lock:
+        st = lib.rz_rasterize_sparse(ctx.handle, ctypes.byref(g), c_vals, c_bands, nb, ctypes.byref(ri),
+                                     _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags, ctypes.byref(h),
+                                     ctypes.byref(st_c), e, len(e))
+    _lib.raise_for(st, e.value)
+    try:
+        v = _lib.RzSparseView()
+        lib.rz_sparse_view_get(h, ctypes.byref(v))
+        n = int(v.count)
+
+        def arr(ptr, count, dt):
+            if count == 0:
+                return np.empty(0, dtype=dt)
+            return np.frombuffer(ctypes.string_at(ptr, count * np.dtype(dt).itemsize), dtype=dt).copy()
+
+        band_counts = arr(v.band_counts, int(v.n_bands), np.uint64)
+        rows = arr(v.rows, n, np.uint64)
+        cols = arr(v.cols, n, np.uint64)
+        vals = arr(v.values, n, np_dt)
+    finally:
+        lib.rz_sparse_free(h)
+    if stats is not None:
+        stats.update(st_c.as_dict())
+    return band_counts, rows, cols, vals
+
