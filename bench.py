@@ -226,8 +226,14 @@ def run_gb300(args) -> None:
     launches = sum(s1["kernel_launches"] + s2["kernel_launches"] for s1, s2 in acc)
     phase = {k: float(np.mean([s1[k] + s2[k] for s1, s2 in acc]))
              for k in ("ms_prep", "ms_spans", "ms_bucket", "ms_fill")}
-    fill_bytes = acc[0][0]["out_bytes"] + acc[0][1]["out_bytes"]
-    span_bytes = 8 * (acc[0][0]["spans"] + acc[0][1]["spans"])
+    # algorithmic bytes of one step's phases (both calls):
+    #   fill  : the dense rasters written + every coverage record read (8 B)
+    #           + the gathered f64 value of each record of the sum call (8 B)
+    #   spans : the vertex table read (16 B per vertex and call) + every
+    #           coverage record written (wid, part, mask: 12 B)
+    recs_sum, recs_cnt = acc[0][0]["spans"], acc[0][1]["spans"]
+    fill_bytes = acc[0][0]["out_bytes"] + acc[0][1]["out_bytes"] + 8 * (recs_sum + recs_cnt) + 8 * recs_sum
+    span_bytes = 2 * 16 * w.table.n_vertices + 12 * (recs_sum + recs_cnt)
     if world > 1:
         t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -275,17 +281,16 @@ def run_gb300(args) -> None:
     peaks = _measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     # dominant kernel phase: the larger of span generation and fill
-    if phase["ms_fill"] >= phase["ms_spans"]:
-        dom, dom_ms, dom_bytes = "fill (k_fill_small/k_fill_big)", phase["ms_fill"], fill_bytes + span_bytes
-    else:
-        dom = "span generation (k_poly_spans)"
-        dom_ms = phase["ms_spans"]
-        dom_bytes = 2 * 16 * w.table.n_vertices + 12 * (acc[0][0]["spans"] + acc[0][1]["spans"])
+    phases = {"spans": ("span generation (k_poly_spans_narrow, k_poly_spans)", phase["ms_spans"], span_bytes),
+              "fill": ("fill (k_fill_warp, k_fill_big, k_fill_depth)", phase["ms_fill"], fill_bytes)}
+    dom_key = max(phases, key=lambda k: phases[k][1])
+    dom, dom_ms, dom_bytes = phases[dom_key]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": None,
                 "peak_source": "measured" if not peaks.get("fallback") else "fallback",
-                "fill_gbs": (fill_bytes + span_bytes) / (phase["ms_fill"] / 1e3) / 1e9,
+                "algorithmic_bytes_per_step": {"spans": span_bytes, "fill": fill_bytes},
+                "gbs_per_phase": {k: v[2] / (v[1] / 1e3) / 1e9 for k, v in phases.items()},
                 "phase_ms": phase}
 
     cpu = None
