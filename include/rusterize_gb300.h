@@ -225,6 +225,48 @@ rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, const void* va
 rz_status rz_sparse_view_get(const rz_sparse* sp, rz_sparse_view* out);
 void rz_sparse_free(rz_sparse* sp);
 
+/* ---- batches of independent jobs ---------------------------------------- */
+
+/* One job of a batch: the arguments of one single-band rz_rasterize call. */
+typedef struct {
+  rz_geoms geoms;          /* host arrays, or device arrays with RZ_FLAG_INPUT_DEVICE
+                              on the batch; xy of device jobs 16-byte aligned */
+  const void* values;      /* per-geometry values of the batch dtype (host or
+                              device, like geoms), ONE host value with
+                              RZ_FLAG_SCALAR_VALUE in `flags`, or NULL (T::one()) */
+  const void* background;  /* one host value of the batch dtype */
+  rz_raster_info info;
+  rz_pixel_fn fn;
+  uint32_t flags;          /* RZ_FLAG_SCALAR_VALUE */
+  void* out;               /* nrows * ncols values (C order): host memory, or
+                              device memory with RZ_FLAG_OUTPUT_DEVICE */
+} rz_job;
+
+typedef struct {
+  uint64_t jobs, waves;
+  uint64_t edges, records, pixel_writes, out_bytes;
+  uint32_t kernel_launches, reruns;
+  float ms_device_total; /* CUDA events around every wave, summed */
+  float ms_host_total;
+} rz_batch_stats;
+
+/* No single counterpart in the reference, which burns one raster per call
+ * (Rasterize::rasterize, rust/src/rasterize.rs:54-116): this runs many
+ * independent jobs -- each with its own geometries, raster, pixel function
+ * and background, all with output type `out_dtype` -- through one pass of
+ * the engine's kernels per wave instead of one pass per job.  Every job's
+ * raster is bit-identical to what rz_rasterize returns for it alone.
+ *
+ * Jobs are grouped, in order, into waves whose device footprint (rasters,
+ * when they are not device outputs, plus geometry tables) stays within
+ * `wave_bytes` (0: 8 GiB); a job larger than that runs as a wave of its own.
+ * `flags`: RZ_FLAG_INPUT_DEVICE, RZ_FLAG_OUTPUT_DEVICE, RZ_FLAG_ALL_TOUCHED
+ * (for every job), RZ_FLAG_NO_TIMING.  The call returns after every output
+ * is written. */
+rz_status rz_rasterize_batch(rz_context* ctx, const rz_job* jobs, size_t n_jobs, rz_dtype out_dtype,
+                             uint32_t flags, uint64_t wave_bytes, rz_batch_stats* stats, char* err,
+                             size_t errlen);
+
 /* The context's CUDA stream (a cudaStream_t), e.g. to record CUDA events
  * around calls or to order other work after them. */
 void* rz_context_stream(rz_context* ctx);

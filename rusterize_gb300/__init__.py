@@ -25,7 +25,7 @@ from ._dependencies import polars as pl
 from ._dependencies import xarray as xr
 from ._lib import Context, EngineError, NoDeviceError, PanicException, default_context
 from ._native import _rusterize, group_keys, parse_geometry
-from .engine import RasterInfo, raster_info, rasterize_table, rasterize_table_sparse
+from .engine import BatchJob, RasterInfo, raster_info, rasterize_batch, rasterize_table, rasterize_table_sparse
 from .geometry import GeometryTable, TableBuilder, from_wkb, from_wkt
 from .sparse import SparseArray
 
@@ -33,7 +33,8 @@ __version__ = "0.1.0"
 
 __all__ = [
     "rusterize", "_rusterize", "GeometryTable", "TableBuilder", "from_wkt", "from_wkb", "RasterInfo",
-    "raster_info", "rasterize_table", "rasterize_table_sparse", "SparseArray", "group_keys", "parse_geometry", "Context", "default_context",
+    "raster_info", "rasterize_table", "rasterize_table_sparse", "rasterize_batch", "BatchJob", "SparseArray",
+    "group_keys", "parse_geometry", "Context", "default_context",
     "PanicException", "EngineError", "NoDeviceError",
 ]
 

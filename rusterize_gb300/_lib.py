@@ -82,6 +82,24 @@ class RzStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class RzJob(ctypes.Structure):
+    _fields_ = [
+        ("geoms", RzGeoms), ("values", c_void_p), ("background", c_void_p), ("info", RzRasterInfo),
+        ("fn", c_int), ("flags", c_uint32), ("out", c_void_p),
+    ]
+
+
+class RzBatchStats(ctypes.Structure):
+    _fields_ = [
+        ("jobs", c_uint64), ("waves", c_uint64), ("edges", c_uint64), ("records", c_uint64),
+        ("pixel_writes", c_uint64), ("out_bytes", c_uint64), ("kernel_launches", c_uint32), ("reruns", c_uint32),
+        ("ms_device_total", c_float), ("ms_host_total", c_float),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class RzSparseView(ctypes.Structure):
     _fields_ = [
         ("count", c_uint64), ("n_bands", c_uint32), ("dtype", c_int),
@@ -116,6 +134,8 @@ PROTOTYPES = {
                                     c_int, c_int, c_uint32, POINTER(c_void_p), POINTER(RzStats), c_char_p, c_size_t]),
     "rz_sparse_view_get": (c_int, [c_void_p, POINTER(RzSparseView)]),
     "rz_sparse_free": (None, [c_void_p]),
+    "rz_rasterize_batch": (c_int, [c_void_p, POINTER(RzJob), c_size_t, c_int, c_uint32, c_uint64,
+                                   POINTER(RzBatchStats), c_char_p, c_size_t]),
 }
 
 _lib = None

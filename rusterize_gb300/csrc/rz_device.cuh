@@ -68,6 +68,7 @@ enum : unsigned {
   ERR_BITMAP = 4,      // crossing outside its part's bitmap (non-finite geometry)
   ERR_TOO_WIDE = 5,    // polygon part wider than the bitmap
   ERR_LINE_LONG = 6,   // segment needs more than LINE_MAX_STEPS steps
+  ERR_BAD_JOB = 7,     // a batch job's table does not start at 0 / end at its counts
 };
 
 // Device control block, reset at the start of every pass.
@@ -85,15 +86,27 @@ struct Ctrl {
   unsigned long long pad[8];
 };
 
+// The world -> pixel map of the call (edges.rs:94-97).  A batch of jobs
+// maps every job's vertices to pixels first (k_batch_vertices) and then runs
+// with the identity map: xmin = +0, ymax = -0, resolution 1 and the pixel y
+// stored negated, which gives back every pixel coordinate bit for bit.
 struct Grid {
   double xmin, ymax, xres, yres, inv_xres, inv_yres;
   int pow2_x, pow2_y;  // resolution a power of two: multiply by the exact reciprocal
   int unit_x, unit_y;  // resolution 1: the division is the identity
+  int touched;         // all_touched: lines and polygon rings take the AllTouched walk
+};
+
+// The raster a part burns into, per job of a call (one entry for a single
+// call): its size, where its record words start, and the record flags of its
+// line and polygon parts.
+struct JobDims {
   int nrows, ncols;
-  unsigned ntx;      // column tiles per row
-  unsigned n_bands;
-  int touched;          // all_touched: lines and polygon rings take the AllTouched walk
-  unsigned poly_flags;  // flags of polygon fill records (DEDUP_BIT: the part's pixels are a set)
+  unsigned ntx;        // 512-pixel column tiles per row
+  unsigned wid_base;   // first record word id of the job's raster
+  unsigned line_flag;  // DEDUP_BIT: line parts write each pixel once (PixelCache)
+  unsigned poly_flag;  // DEDUP_BIT: polygon parts write each pixel once (all_touched sum / count)
+  unsigned long long geom0;  // first geometry of the job
 };
 
 struct Geo {
@@ -103,6 +116,7 @@ struct Geo {
   const unsigned long long* vertex_offsets;
   const double2* xy;
   const unsigned* bands;  // per geometry, or nullptr
+  const unsigned char* ring_closed = nullptr;  // per ring: LineString::is_closed of the world coordinates, or nullptr (taken from xy)
   unsigned long long n_geoms, n_parts, n_rings, n_vertices;
 };
 
@@ -113,6 +127,11 @@ struct PartPlan {
   int bw;          // bitmap words per row
   int wr;          // rows per window
   unsigned band;   // output band of the part
+  int nrows, ncols;  // the part's raster
+  unsigned wid0;     // record word id of (band, row 0) in the part's raster
+  unsigned wpr;      // record words per raster row (ntx * WPT)
+  unsigned flags;    // flags of the part's records (DEDUP_BIT)
+  unsigned pad;
 };
 
 // Part-level counters, scanned (exclusive) into offsets: polygon windows of
@@ -175,13 +194,22 @@ __device__ __forceinline__ long long as_isize(double v) {
   return (long long)v;
 }
 
-// Emit the run [xs, xe) of row `y` in `band` for `part` as coverage
+// The job of geometry `gi`: the last job whose first geometry is <= gi.
+__device__ __forceinline__ unsigned job_of(const JobDims* jobs, unsigned n_jobs, unsigned long long gi) {
+  unsigned lo = 0, hi = n_jobs;  // jobs[lo].geom0 <= gi < jobs[hi].geom0
+  while (hi - lo > 1) {
+    const unsigned mid = (lo + hi) >> 1;
+    if (jobs[mid].geom0 <= gi) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Emit the run [xs, xe) of row `y` of the part planned in `pl` as coverage
 // records, one per 32-pixel word.  Slots are taken with warp-aggregated
 // atomics.
-__device__ __forceinline__ void emit_run(const RecBuf& rb, unsigned* bucket_count, Ctrl* ctrl, const Grid& g,
-                                         unsigned band, int y, int xs, int xe, unsigned part_flags) {
-  const unsigned long long rowid = (unsigned long long)band * (unsigned)g.nrows + (unsigned)y;
-  const unsigned row_wid = (unsigned)(rowid * g.ntx * WPT);
+__device__ __forceinline__ void emit_run(const RecBuf& rb, unsigned* bucket_count, Ctrl* ctrl, const PartPlan& pl,
+                                         int y, int xs, int xe, unsigned part_flags) {
+  const unsigned row_wid = pl.wid0 + (unsigned)y * pl.wpr;
   for (int wd = xs >> 5; (wd << 5) < xe; ++wd) {
     const int lo = max(xs, wd << 5) - (wd << 5), hi = min(xe, (wd << 5) + 32) - (wd << 5);
     const unsigned mask = (hi == 32 ? 0xFFFFFFFFu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);

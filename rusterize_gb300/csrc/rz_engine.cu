@@ -11,7 +11,9 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <thread>
 
+#include "rz_batch.cuh"
 #include "rz_device.cuh"
 #include "rz_fill.cuh"
 #include "rz_internal.h"
@@ -108,6 +110,138 @@ unsigned grid_for(unsigned long long work, unsigned per_block, unsigned cap) {
   return (unsigned)g;
 }
 
+// The status and message of an error a kernel recorded in the control block.
+rz_status ctrl_error(const Ctrl& hc, char* err, size_t errlen) {
+  const unsigned long long ix = hc.err_index;
+  switch (hc.err) {
+    case ERR_BAD_TABLE:
+      return fail(err, errlen, RZ_INVALID_ARGUMENT, "geometry table is inconsistent (%s offsets, index %llu)",
+                  (ix >> 62) == 0 ? "part" : ((ix >> 62) == 1 ? "ring" : "vertex"), ix & ((1ull << 62) - 1));
+    case ERR_BAD_KIND: return fail(err, errlen, RZ_INVALID_ARGUMENT, "invalid part kind at part %llu", ix);
+    case ERR_BAD_BAND: return fail(err, errlen, RZ_INVALID_ARGUMENT, "band index out of range at geometry %llu", ix);
+    case ERR_BITMAP:
+      return fail(err, errlen, RZ_RUNTIME_ERROR, "polygon part %llu has non-finite or out-of-range coordinates", ix);
+    case ERR_TOO_WIDE:
+      return fail(err, errlen, RZ_VALUE_ERROR, "polygon part %llu is wider than %d raster columns", ix,
+                  BITMAP_WORDS * 32 - 64);
+    case ERR_LINE_LONG:
+      return fail(err, errlen, RZ_VALUE_ERROR, "line segment at vertex %llu spans more than 2^26 pixels", ix);
+    case ERR_BAD_JOB:
+      return fail(err, errlen, RZ_INVALID_ARGUMENT,
+                  "geometry table of job %llu does not start at 0 or end at its own counts", ix);
+    default: return fail(err, errlen, RZ_RUNTIME_ERROR, "engine error %u", hc.err);
+  }
+}
+
+// The world -> pixel map of one raster (edges.rs:94-97).
+Grid make_grid(const rz_raster_info* info, bool touched) {
+  Grid gr;
+  gr.xmin = info->xmin;
+  gr.ymax = info->ymax;
+  gr.xres = info->xres;
+  gr.yres = info->yres;
+  gr.pow2_x = is_pow2(info->xres);
+  gr.pow2_y = is_pow2(info->yres);
+  gr.inv_xres = gr.pow2_x ? 1.0 / info->xres : 0.0;
+  gr.inv_yres = gr.pow2_y ? 1.0 / info->yres : 0.0;
+  gr.unit_x = info->xres == 1.0;
+  gr.unit_y = info->yres == 1.0;
+  gr.touched = touched ? 1 : 0;
+  return gr;
+}
+
+// PixelCache use (burn_geometry.rs:179-185, 212-243; prelude.rs:116-118):
+// the writes of a part are deduplicated for sum / count when the pixels are
+// not square (line parts) or all_touched is on (line and polygon parts).
+bool fill_dedup(const rz_raster_info* info, rz_pixel_fn fn, bool touched) {
+  return (info->xres != info->yres || touched) && (fn == RZ_SUM || fn == RZ_COUNT);
+}
+
+// The raster of one job.  The sparse stream also drops the repeats of
+// non-square line pixels for the other functions, which LineString::burn's
+// PixelCache drops, although the dense result does not depend on them.
+JobDims job_dims(unsigned long long nrows, unsigned long long ncols, const rz_raster_info* info, rz_pixel_fn fn,
+                 bool touched, bool sparse, unsigned wid_base, unsigned long long geom0) {
+  const bool line_dedup = info->xres != info->yres;
+  const bool dedup = fill_dedup(info, fn, touched);
+  JobDims jd;
+  jd.nrows = (int)nrows;
+  jd.ncols = (int)ncols;
+  jd.ntx = (unsigned)((ncols + TW - 1) >> TW_SHIFT);
+  jd.wid_base = wid_base;
+  jd.line_flag = (dedup || (sparse && line_dedup)) ? DEDUP_BIT : 0u;
+  jd.poly_flag = touched && dedup ? DEDUP_BIT : 0u;
+  jd.geom0 = geom0;
+  return jd;
+}
+
+void set_background(FillArgs& fa, unsigned long long bits, size_t tsize) {
+  fa.bg = bits;
+  unsigned char pat[16];
+  for (int i = 0; i < 16; i += (int)tsize) std::memcpy(pat + i, &bits, tsize);
+  std::memcpy(&fa.bg16, pat, 16);
+}
+
+// Device tables of the part map.
+struct PartTables {
+  unsigned* part_geom;
+  PartPlan* plan;
+  unsigned long long* counts;  // [P][PC_N]
+  unsigned long long* poff;    // [P+1][PC_N]
+  unsigned long long* tmp64;   // scan scratch
+  unsigned* line_parts;
+  unsigned* point_parts;
+  unsigned long long* last_kept;
+};
+
+// validate -> part -> geometry -> part plans -> scan -> part lists.  Returns
+// the kernels launched.
+int launch_prep(const Geo& geo, const Grid& gr, const JobDims& one, const JobDims* jobs, unsigned n_jobs,
+                unsigned band_check, const PartTables& t, Ctrl* d_ctrl, int sms, cudaStream_t s) {
+  const unsigned long long G = geo.n_geoms, P = geo.n_parts, R = geo.n_rings;
+  int launches = 0;
+  const unsigned long long maxn = std::max({G + 1, P + 1, R + 1});
+  k_validate<<<grid_for(maxn, 256, sms * 8), 256, 0, s>>>(geo, d_ctrl);
+  ++launches;
+  if (band_check && G) {
+    k_check_bands<<<grid_for(G, 256, sms * 8), 256, 0, s>>>(geo, band_check, d_ctrl);
+    ++launches;
+  }
+  if (G) {
+    k_part_geom<<<grid_for(G, 256, sms * 16), 256, 0, s>>>(geo, t.part_geom, d_ctrl);
+    ++launches;
+  }
+  if (P) {
+    k_part_prep<<<grid_for(P, 8, sms * 32), 256, 0, s>>>(geo, gr, one, jobs, n_jobs, t.part_geom, t.plan, t.counts,
+                                                         d_ctrl);
+    ++launches;
+  }
+  launches += scan<unsigned long long, PC_N>(t.counts, t.poff, P, t.tmp64, s);
+  if (P) {
+    k_part_lists<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(geo, t.poff, t.line_parts, t.point_parts, d_ctrl);
+    ++launches;
+  }
+  return launches;
+}
+
+// Coverage records of every part kind.  Returns the kernels launched.
+int launch_coverage(const Geo& geo, const Grid& gr, const PartTables& t, const RecBuf& sb, unsigned* bcount,
+                    Ctrl* d_ctrl, int sms, int narrow_bps, int poly_bps, cudaStream_t s) {
+  if (!geo.n_parts) return 0;
+  k_poly_spans_narrow<<<sms * narrow_bps, SMALL_WARPS * 32, SMALL_SMEM, s>>>(geo, gr, t.plan, t.poff, sb, bcount,
+                                                                             d_ctrl);
+  k_poly_spans<<<sms * poly_bps, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, t.plan, t.poff, sb, bcount, d_ctrl);
+  k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, t.plan, t.poff, t.line_parts, t.last_kept, sb, bcount, d_ctrl);
+  int launches = 4;
+  if (!gr.touched) {  // AllTouched writes no separate end pixel
+    k_line_endpix<<<grid_for(geo.n_parts, 256, sms * 4), 256, 0, s>>>(geo, gr, t.plan, t.poff, t.line_parts,
+                                                                       t.last_kept, sb, bcount, d_ctrl);
+    ++launches;
+  }
+  k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, t.plan, t.poff, t.point_parts, sb, bcount, d_ctrl);
+  return launches;
+}
+
 }  // namespace
 
 // Host copy of a sparse (COO) result.
@@ -124,10 +258,12 @@ struct rz_context {
   int poly_blocks_per_sm = 1;
   int narrow_blocks_per_sm = 1;
   cudaStream_t stream = nullptr;
-  DevBuf main, spans, out, sparse;
+  DevBuf main, spans, out, sparse, batch, stage;
   cudaEvent_t ev[8] = {};
   Ctrl* h_ctrl = nullptr;  // pinned
   unsigned long long span_cap_hint = 0;
+  unsigned char* h_stage = nullptr;  // pinned staging of batch tables and host job inputs
+  size_t h_stage_cap = 0;
 };
 
 extern "C" const char* rz_build_info(void) {
@@ -194,11 +330,12 @@ extern "C" void rz_context_destroy(rz_context* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out, &ctx->sparse})
+  for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out, &ctx->sparse, &ctx->batch, &ctx->stage})
     if (b->p) cudaFree(b->p);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->h_ctrl) cudaFreeHost(ctx->h_ctrl);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -207,11 +344,14 @@ extern "C" rz_status rz_context_trim(rz_context* ctx) {
   if (!ctx) return RZ_INVALID_ARGUMENT;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out, &ctx->sparse}) {
+  for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out, &ctx->sparse, &ctx->batch, &ctx->stage}) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
     b->cap = 0;
   }
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  ctx->h_stage = nullptr;
+  ctx->h_stage_cap = 0;
   ctx->span_cap_hint = 0;
   return RZ_OK;
 }
@@ -362,34 +502,10 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   }
   if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[1], s));
 
-  Grid gr;
-  gr.xmin = info->xmin;
-  gr.ymax = info->ymax;
-  gr.xres = info->xres;
-  gr.yres = info->yres;
-  gr.pow2_x = is_pow2(info->xres);
-  gr.pow2_y = is_pow2(info->yres);
-  gr.inv_xres = gr.pow2_x ? 1.0 / info->xres : 0.0;
-  gr.inv_yres = gr.pow2_y ? 1.0 / info->yres : 0.0;
-  gr.unit_x = info->xres == 1.0;
-  gr.unit_y = info->yres == 1.0;
-  gr.nrows = (int)nrows;
-  gr.ncols = (int)ncols;
-  gr.ntx = ntx;
-  gr.n_bands = (unsigned)nb;
-  // LineString::burn uses a PixelCache when pixels are not square
-  // (burn_geometry.rs:179-185): writes of such a part are deduplicated.
-  const bool line_dedup = info->xres != info->yres;
-  // all_touched: a part's pixels form a set (PixelCache for sum / count,
-  // prelude.rs:116-118; repeated writes of one value for the others)
   const bool touched = (flags & RZ_FLAG_ALL_TOUCHED) != 0;
-  const bool dedup = (line_dedup || touched) && (fn == RZ_SUM || fn == RZ_COUNT);
-  gr.touched = touched ? 1 : 0;
-  gr.poly_flags = touched && dedup ? DEDUP_BIT : 0u;
-  // lines: a dense raster only needs the PixelCache where a repeated write
-  // changes the pixel (sum / count); the triplet stream of the sparse
-  // encoding drops every repeat the cache drops (burn_geometry.rs:179-185)
-  const unsigned line_flag = (dedup || (sp && line_dedup)) ? DEDUP_BIT : 0u;
+  const Grid gr = make_grid(info, touched);
+  const JobDims one = job_dims(nrows, ncols, info, fn, touched, sp != nullptr, 0u, 0ull);
+  const bool dedup = fill_dedup(info, fn, touched);
 
   Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
   unsigned* part_geom = static_cast<unsigned*>(at(o_pg));
@@ -408,26 +524,16 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
 
   // ---- prep ----
   RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
-  const unsigned long long maxn = std::max({G + 1, P + 1, R + 1});
-  k_validate<<<grid_for(maxn, 256, sms * 8), 256, 0, s>>>(geo, d_ctrl);
-  ++launches;
-  if (band_of_geom && G) {
-    k_check_bands<<<grid_for(G, 256, sms * 8), 256, 0, s>>>(geo, (unsigned)nb, d_ctrl);
-    ++launches;
-  }
-  if (G) {
-    k_part_geom<<<grid_for(G, 256, sms * 16), 256, 0, s>>>(geo, part_geom, d_ctrl);
-    ++launches;
-  }
-  if (P) {
-    k_part_prep<<<grid_for(P, 8, sms * 32), 256, 0, s>>>(geo, gr, part_geom, plan, counts, d_ctrl);
-    ++launches;
-  }
-  launches += scan<unsigned long long, PC_N>(counts, poff, P, static_cast<unsigned long long*>(at(o_tmp64)), s);
-  if (P) {
-    k_part_lists<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(geo, poff, line_parts, point_parts, d_ctrl);
-    ++launches;
-  }
+  PartTables pt;
+  pt.part_geom = part_geom;
+  pt.plan = plan;
+  pt.counts = counts;
+  pt.poff = poff;
+  pt.tmp64 = static_cast<unsigned long long*>(at(o_tmp64));
+  pt.line_parts = line_parts;
+  pt.point_parts = point_parts;
+  pt.last_kept = last_kept;
+  launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sms, s);
   RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
   if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[2], s));
 
@@ -447,19 +553,8 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
     RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
     launches += 1;
-    if (P) {
-      k_poly_spans_narrow<<<sms * ctx->narrow_blocks_per_sm, SMALL_WARPS * 32, SMALL_SMEM, s>>>(
-          geo, gr, plan, poff, sb, bcount, d_ctrl);
-      k_poly_spans<<<sms * ctx->poly_blocks_per_sm, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, plan, poff, sb, bcount,
-                                                                                  d_ctrl);
-      k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept, line_flag, sb,
-                                           bcount, d_ctrl);
-      if (!touched)
-        k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
-                                                                 line_flag, sb, bcount, d_ctrl);
-      k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, point_parts, sb, bcount, d_ctrl);
-      launches += 5;
-    }
+    launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sms, ctx->narrow_blocks_per_sm,
+                                ctx->poly_blocks_per_sm, s);
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[3], s));
     if (!sp) {
     launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
@@ -473,18 +568,18 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     fa.nbuckets = nbuckets;
     fa.scalar = scalar_bits;
     fa.out = d_out;
-    fa.bg = bg_bits;
-    {
-      unsigned char pat[16];
-      for (int i = 0; i < 16; i += (int)tsize) std::memcpy(pat + i, &bg_bits, tsize);
-      std::memcpy(&fa.bg16, pat, 16);
-    }
+    set_background(fa, bg_bits, tsize);
     fa.nrows = (int)nrows;
     fa.ncols = (int)ncols;
     fa.ntx = ntx;
     fa.big = big;
     fa.ctrl = d_ctrl;
     fa.rec_cap = cap;
+    fa.work = &d_ctrl->fill_work;
+    fa.nbig = &d_ctrl->big_count;
+    fa.jobs = nullptr;
+    fa.n_jobs = 0;
+    fa.bucket0 = 0;
     launches += fill(fa, (int)fn, dedup, sms, s);
     }
     RZ_CUDA(cudaGetLastError());
@@ -495,26 +590,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     RZ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
     RZ_CUDA(cudaStreamSynchronize(s));
     const Ctrl& hc = *ctx->h_ctrl;
-    if (hc.err) {
-      const unsigned long long ix = hc.err_index;
-      switch (hc.err) {
-        case ERR_BAD_TABLE:
-          return fail(err, errlen, RZ_INVALID_ARGUMENT,
-                      "geometry table is inconsistent (%s offsets, index %llu)",
-                      (ix >> 62) == 0 ? "part" : ((ix >> 62) == 1 ? "ring" : "vertex"), ix & ((1ull << 62) - 1));
-        case ERR_BAD_KIND: return fail(err, errlen, RZ_INVALID_ARGUMENT, "invalid part kind at part %llu", ix);
-        case ERR_BAD_BAND: return fail(err, errlen, RZ_INVALID_ARGUMENT, "band index out of range at geometry %llu", ix);
-        case ERR_BITMAP:
-          return fail(err, errlen, RZ_RUNTIME_ERROR,
-                      "polygon part %llu has non-finite or out-of-range coordinates", ix);
-        case ERR_TOO_WIDE:
-          return fail(err, errlen, RZ_VALUE_ERROR, "polygon part %llu is wider than %d raster columns", ix,
-                      BITMAP_WORDS * 32 - 64);
-        case ERR_LINE_LONG:
-          return fail(err, errlen, RZ_VALUE_ERROR, "line segment at vertex %llu spans more than 2^26 pixels", ix);
-        default: return fail(err, errlen, RZ_RUNTIME_ERROR, "engine error %u", hc.err);
-      }
-    }
+    if (hc.err) return ctrl_error(hc, err, errlen);
     if (hc.span_count > cap) {
       unsigned long long want = hc.span_count + hc.span_count / 4 + 1024;
       if (want > 0xFFFFFFF0ull) {
@@ -544,7 +620,6 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     sbr.wid = static_cast<unsigned*>(ctx->spans.p);
     sbr.part = sbr.wid + cap;
     sbr.mask = sbr.part + cap;
-    const unsigned wpr = ntx * WPT;
     const unsigned long long nsort = std::max<unsigned long long>(n, nb > 1 ? P : 0);
     Layout SL;
     const size_t o_k0 = SL.take(8 * (nsort ? nsort : 1)), o_k1 = SL.take(8 * (nsort ? nsort : 1));
@@ -583,7 +658,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     unsigned long long* bcnt = static_cast<unsigned long long*>(sat(o_bc));
     RZ_CUDA(cudaMemsetAsync(bcnt, 0, 8 * nb, s));
     if (n) {
-      k_rec_keys<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(sbr, n, prank, plan, (unsigned)(nrows * wpr), k0, v0);
+      k_rec_keys<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(sbr, n, prank, plan, k0, v0);
       const bool in_tmp = radix_sort(k0, v0, k1, v1, (unsigned)n, 32 + bits_part,
                                      static_cast<unsigned*>(sat(o_rst)), s, launches);
       skeys = in_tmp ? k1 : k0;
@@ -624,13 +699,13 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
         void* tvals = sat(o_vals);
         const unsigned eg = grid_for(n, 256, sms * 16);
         switch (tsize) {
-          case 1: k_sparse_emit<1><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, wpr, d_values, part_geom,
+          case 1: k_sparse_emit<1><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
                                                       scalar_bits, trows, tcols, tvals, bcnt); break;
-          case 2: k_sparse_emit<2><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, wpr, d_values, part_geom,
+          case 2: k_sparse_emit<2><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
                                                       scalar_bits, trows, tcols, tvals, bcnt); break;
-          case 4: k_sparse_emit<4><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, wpr, d_values, part_geom,
+          case 4: k_sparse_emit<4><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
                                                       scalar_bits, trows, tcols, tvals, bcnt); break;
-          default: k_sparse_emit<8><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, wpr, d_values,
+          default: k_sparse_emit<8><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values,
                                                        part_geom, scalar_bits, trows, tcols, tvals, bcnt); break;
         }
         ++launches;
@@ -838,26 +913,11 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   geo.xy = reinterpret_cast<const double2*>(g->xy);
   geo.bands = band_of_geom;
 
-  Grid gr;
-  gr.xmin = info->xmin;
-  gr.ymax = info->ymax;
-  gr.xres = info->xres;
-  gr.yres = info->yres;
-  gr.pow2_x = is_pow2(info->xres);
-  gr.pow2_y = is_pow2(info->yres);
-  gr.inv_xres = gr.pow2_x ? 1.0 / info->xres : 0.0;
-  gr.inv_yres = gr.pow2_y ? 1.0 / info->yres : 0.0;
-  gr.unit_x = info->xres == 1.0;
-  gr.unit_y = info->yres == 1.0;
-  gr.nrows = (int)nrows;
-  gr.ncols = (int)ncols;
-  gr.ntx = ntx;
-  gr.n_bands = (unsigned)nb;
   // PixelCache semantics as in rz_rasterize
   const bool touched = (flags & RZ_FLAG_ALL_TOUCHED) != 0;
-  const bool dedup = (info->xres != info->yres || touched) && (fn == RZ_SUM || fn == RZ_COUNT);
-  gr.touched = touched ? 1 : 0;
-  gr.poly_flags = touched && dedup ? DEDUP_BIT : 0u;
+  const Grid gr = make_grid(info, touched);
+  const JobDims one = job_dims(nrows, ncols, info, fn, touched, false, 0u, 0ull);
+  const bool dedup = fill_dedup(info, fn, touched);
 
   Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
   unsigned* part_geom = static_cast<unsigned*>(at(o_pg));
@@ -874,26 +934,16 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   int launches = 0;
 
   RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
-  const unsigned long long maxn = std::max({G + 1, P + 1, R + 1});
-  k_validate<<<grid_for(maxn, 256, sms * 8), 256, 0, s>>>(geo, d_ctrl);
-  ++launches;
-  if (band_of_geom && G) {
-    k_check_bands<<<grid_for(G, 256, sms * 8), 256, 0, s>>>(geo, (unsigned)nb, d_ctrl);
-    ++launches;
-  }
-  if (G) {
-    k_part_geom<<<grid_for(G, 256, sms * 16), 256, 0, s>>>(geo, part_geom, d_ctrl);
-    ++launches;
-  }
-  if (P) {
-    k_part_prep<<<grid_for(P, 8, sms * 32), 256, 0, s>>>(geo, gr, part_geom, plan, counts, d_ctrl);
-    ++launches;
-  }
-  launches += scan<unsigned long long, PC_N>(counts, poff, P, static_cast<unsigned long long*>(at(o_tmp64)), s);
-  if (P) {
-    k_part_lists<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(geo, poff, line_parts, point_parts, d_ctrl);
-    ++launches;
-  }
+  PartTables pt;
+  pt.part_geom = part_geom;
+  pt.plan = plan;
+  pt.counts = counts;
+  pt.poff = poff;
+  pt.tmp64 = static_cast<unsigned long long*>(at(o_tmp64));
+  pt.line_parts = line_parts;
+  pt.point_parts = point_parts;
+  pt.last_kept = last_kept;
+  launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sms, s);
   RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
   RecBuf sb;
   sb.cap = cap;
@@ -905,18 +955,7 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
   RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
   ++launches;
-  if (P) {
-    k_poly_spans_narrow<<<sms * nd.narrow_bps, SMALL_WARPS * 32, SMALL_SMEM, s>>>(geo, gr, plan, poff, sb, bcount,
-                                                                                   d_ctrl);
-    k_poly_spans<<<sms * nd.poly_bps, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, plan, poff, sb, bcount, d_ctrl);
-    k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept, dedup ? DEDUP_BIT : 0u, sb,
-                                         bcount, d_ctrl);
-    if (!touched)
-      k_line_endpix<<<grid_for(P, 256, sms * 4), 256, 0, s>>>(geo, gr, plan, poff, line_parts, last_kept,
-                                                               dedup ? DEDUP_BIT : 0u, sb, bcount, d_ctrl);
-    k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, plan, poff, point_parts, sb, bcount, d_ctrl);
-    launches += 5;
-  }
+  launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sms, nd.narrow_bps, nd.poly_bps, s);
   launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
   const void* d_vals_na = per_geom_values ? values : nullptr;
   launch_scatter(tsize, sms, s, sb, boff, bcount, sorted, d_vals_na, part_geom, rvals, d_ctrl);
@@ -928,41 +967,24 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   fa.nbuckets = nbuckets;
   fa.scalar = scalar_bits;
   fa.out = out;
-  fa.bg = bg_bits;
-  {
-    unsigned char pat[16];
-    for (int i = 0; i < 16; i += (int)tsize) std::memcpy(pat + i, &bg_bits, tsize);
-    std::memcpy(&fa.bg16, pat, 16);
-  }
+  set_background(fa, bg_bits, tsize);
   fa.nrows = (int)nrows;
   fa.ncols = (int)ncols;
   fa.ntx = ntx;
   fa.big = big;
   fa.ctrl = d_ctrl;
   fa.rec_cap = cap;
+  fa.work = &d_ctrl->fill_work;
+  fa.nbig = &d_ctrl->big_count;
+  fa.jobs = nullptr;
+  fa.n_jobs = 0;
+  fa.bucket0 = 0;
   launches += fill_for(dt)(fa, (int)fn, dedup, sms, s);
   RZ_CUDA(cudaGetLastError());
   Ctrl hc;  // the caller's stack, no pinned buffer
   RZ_CUDA(cudaMemcpyAsync(&hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
   RZ_CUDA(cudaStreamSynchronize(s));
-  if (hc.err) {
-    const unsigned long long ix = hc.err_index;
-    switch (hc.err) {
-      case ERR_BAD_TABLE:
-        return fail(err, errlen, RZ_INVALID_ARGUMENT, "geometry table is inconsistent (%s offsets, index %llu)",
-                    (ix >> 62) == 0 ? "part" : ((ix >> 62) == 1 ? "ring" : "vertex"), ix & ((1ull << 62) - 1));
-      case ERR_BAD_KIND: return fail(err, errlen, RZ_INVALID_ARGUMENT, "invalid part kind at part %llu", ix);
-      case ERR_BAD_BAND: return fail(err, errlen, RZ_INVALID_ARGUMENT, "band index out of range at geometry %llu", ix);
-      case ERR_BITMAP:
-        return fail(err, errlen, RZ_RUNTIME_ERROR, "polygon part %llu has non-finite or out-of-range coordinates", ix);
-      case ERR_TOO_WIDE:
-        return fail(err, errlen, RZ_VALUE_ERROR, "polygon part %llu is wider than %d raster columns", ix,
-                    BITMAP_WORDS * 32 - 64);
-      case ERR_LINE_LONG:
-        return fail(err, errlen, RZ_VALUE_ERROR, "line segment at vertex %llu spans more than 2^26 pixels", ix);
-      default: return fail(err, errlen, RZ_RUNTIME_ERROR, "engine error %u", hc.err);
-    }
-  }
+  if (hc.err) return ctrl_error(hc, err, errlen);
   if (hc.span_count > cap)
     return fail(err, errlen, RZ_VALUE_ERROR,
                 "job produced %llu spans; the allocation-free entry point holds at most %llu in its %zu-byte "
@@ -977,5 +999,471 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
     stats->buckets = nbuckets;
     stats->kernel_launches = (uint32_t)launches;
   }
+  return RZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches of independent jobs (rz_rasterize_batch).
+//
+// The jobs of a wave are concatenated into one parts table on the device
+// (rz_batch.cuh), so that the whole wave takes one pass of the pipeline: one
+// launch of each kernel instead of one per job, whatever the number and size
+// of the jobs.  Within a wave the jobs are ordered by (pixel function,
+// deduplication, background), so that the buckets of each fill variant are
+// one contiguous range: one fill launch per variant present.
+
+namespace {
+
+struct BatchJob {
+  size_t idx;  // index in the caller's array
+  unsigned long long G, P, R, V, nrows, ncols, ntx, out_elems, buckets;
+  unsigned long long bg_bits, scalar_bits;
+  bool per_geom_values, dedup;
+  rz_pixel_fn fn;
+  size_t dev_bytes;  // device footprint counted against the wave budget
+};
+
+cudaError_t ensure_pinned(rz_context* ctx, size_t need) {
+  if (need <= ctx->h_stage_cap) return cudaSuccess;
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  ctx->h_stage = nullptr;
+  ctx->h_stage_cap = 0;
+  const size_t want = need + need / 4 + (1u << 20);
+  void* p = nullptr;
+  cudaError_t e = cudaMallocHost(&p, want);
+  if (e == cudaSuccess) {
+    ctx->h_stage = static_cast<unsigned char*>(p);
+    ctx->h_stage_cap = want;
+  }
+  return e;
+}
+
+size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+// One wave: jobs[w0..w1) of `order`, already validated.
+rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& wave, rz_dtype dt, uint32_t flags,
+                   rz_batch_stats* stats, char* err, size_t errlen) {
+  const size_t tsize = rz_dtype_size(dt);
+  const bool in_dev = flags & RZ_FLAG_INPUT_DEVICE, out_dev = flags & RZ_FLAG_OUTPUT_DEVICE;
+  const bool touched = flags & RZ_FLAG_ALL_TOUCHED;
+  const bool timing = !(flags & RZ_FLAG_NO_TIMING);
+  cudaStream_t s = ctx->stream;
+  const int sms = ctx->num_sms;
+  // fill variants contiguous (stable: caller order within a variant)
+  std::stable_sort(wave.begin(), wave.end(), [](const BatchJob& a, const BatchJob& b) {
+    if (a.fn != b.fn) return a.fn < b.fn;
+    if (a.dedup != b.dedup) return a.dedup < b.dedup;
+    return a.bg_bits < b.bg_bits;
+  });
+  const unsigned n = (unsigned)wave.size();
+  // ---- wave bases ----
+  std::vector<unsigned long long> base((size_t)BK_N * (n + 1));
+  std::vector<unsigned long long> bucket0(n + 1), out_off(n + 1);
+  for (unsigned j = 0; j <= n; ++j) {
+    for (int k = 0; k < BK_N; ++k) base[(size_t)k * (n + 1) + j] = j ? base[(size_t)k * (n + 1) + j - 1] : 0;
+    bucket0[j] = j ? bucket0[j - 1] : 0;
+    out_off[j] = j ? out_off[j - 1] : 0;
+    if (j) {
+      const BatchJob& b = wave[j - 1];
+      base[(size_t)BK_GEOM * (n + 1) + j] += b.G;
+      base[(size_t)BK_PART * (n + 1) + j] += b.P;
+      base[(size_t)BK_RING * (n + 1) + j] += b.R;
+      base[(size_t)BK_VERT * (n + 1) + j] += b.V;
+      bucket0[j] += b.buckets;
+      out_off[j] += align16(b.out_elems * tsize);
+    }
+  }
+  const unsigned long long Gt = base[(size_t)BK_GEOM * (n + 1) + n], Pt = base[(size_t)BK_PART * (n + 1) + n];
+  const unsigned long long Rt = base[(size_t)BK_RING * (n + 1) + n], Vt = base[(size_t)BK_VERT * (n + 1) + n];
+  const unsigned long long nbuckets = bucket0[n];
+
+  // ---- host staging: job tables, then (host inputs) every job's arrays ----
+  Layout HL;
+  const size_t h_src = HL.take(sizeof(JobSrc) * n), h_dims = HL.take(sizeof(JobDims) * n);
+  const size_t h_fj = HL.take(sizeof(FillJob) * n), h_base = HL.take(8 * base.size());
+  const size_t tables_bytes = HL.off;
+  std::vector<size_t> h_arr(in_dev ? 0 : (size_t)n * 6);
+  if (!in_dev) {
+    for (unsigned j = 0; j < n; ++j) {
+      const BatchJob& b = wave[j];
+      h_arr[6 * j + 0] = HL.take(8 * (b.G + 1));
+      h_arr[6 * j + 1] = HL.take(b.P ? b.P : 1);
+      h_arr[6 * j + 2] = HL.take(8 * (b.P + 1));
+      h_arr[6 * j + 3] = HL.take(8 * (b.R + 1));
+      h_arr[6 * j + 4] = HL.take(16 * (b.V ? b.V : 1));
+      h_arr[6 * j + 5] = HL.take(b.per_geom_values ? tsize * (b.G ? b.G : 1) : 1);
+    }
+  }
+  const size_t stage_bytes = HL.off;
+  RZ_CUDA(ensure_pinned(ctx, stage_bytes));
+  RZ_CUDA(ensure(ctx->stage, stage_bytes));
+  unsigned char* hs = ctx->h_stage;
+  unsigned char* ds = static_cast<unsigned char*>(ctx->stage.p);
+  JobSrc* src = reinterpret_cast<JobSrc*>(hs + h_src);
+  JobDims* dims = reinterpret_cast<JobDims*>(hs + h_dims);
+  FillJob* fj = reinterpret_cast<FillJob*>(hs + h_fj);
+  std::memcpy(hs + h_base, base.data(), 8 * base.size());
+
+  // ---- device wave layout ----
+  Layout L;
+  const size_t o_po = L.take(8 * (Gt + 1)), o_pk = L.take(Pt ? Pt : 1), o_ro = L.take(8 * (Pt + 1));
+  const size_t o_vo = L.take(8 * (Rt + 1)), o_xy = L.take(16 * (Vt ? Vt : 1)), o_val = L.take(tsize * (Gt ? Gt : 1));
+  const size_t o_rc = L.take(Rt ? Rt : 1);
+  const size_t o_pg = L.take(4 * (Pt ? Pt : 1));
+  const size_t o_plan = L.take(sizeof(PartPlan) * (Pt ? Pt : 1));
+  const size_t o_cnt = L.take(8 * PC_N * (Pt ? Pt : 1));
+  const size_t o_poff = L.take(8 * PC_N * (Pt + 1));
+  const size_t o_tmp64 = L.take(8 * scan_temp_elems(Pt, PC_N));
+  const size_t o_last = L.take(8 * (Pt ? Pt : 1));
+  const size_t o_lp = L.take(4 * (Pt ? Pt : 1));
+  const size_t o_pp = L.take(4 * (Pt ? Pt : 1));
+  const size_t o_bc = L.take(4 * (nbuckets ? nbuckets : 1));
+  const size_t o_boff = L.take(4 * (nbuckets + 1));
+  const size_t o_tmp32 = L.take(4 * scan_temp_elems(nbuckets ? nbuckets : 1, 1));
+  const size_t o_big = L.take(4 * (nbuckets ? nbuckets : 1));
+  const size_t o_ctrl = L.take(sizeof(Ctrl));
+  const size_t o_gctr = L.take(16 * (n + 1));
+  RZ_CUDA(ensure(ctx->batch, L.off));
+  if (!out_dev) RZ_CUDA(ensure(ctx->out, out_off[n] ? out_off[n] : 16));
+  char* mb = static_cast<char*>(ctx->batch.p);
+  auto at = [&](size_t o) { return static_cast<void*>(mb + o); };
+
+  // ---- job tables ----
+  const Grid ident = [&] {
+    Grid g;
+    g.xmin = 0.0;
+    g.ymax = -0.0;
+    g.xres = g.yres = 1.0;
+    g.inv_xres = g.inv_yres = 0.0;
+    g.pow2_x = g.pow2_y = 0;
+    g.unit_x = g.unit_y = 1;
+    g.touched = touched ? 1 : 0;
+    return g;
+  }();
+  for (unsigned j = 0; j < n; ++j) {
+    const BatchJob& b = wave[j];
+    const rz_job& jb = jobs[b.idx];
+    JobSrc& sj = src[j];
+    sj.n_geoms = b.G;
+    sj.n_parts = b.P;
+    sj.n_rings = b.R;
+    sj.n_vertices = b.V;
+    sj.grid = make_grid(&jb.info, touched);
+    sj.scalar = b.scalar_bits;
+    if (in_dev) {
+      sj.part_offsets = reinterpret_cast<const unsigned long long*>(jb.geoms.part_offsets);
+      sj.part_kind = jb.geoms.part_kind;
+      sj.ring_offsets = reinterpret_cast<const unsigned long long*>(jb.geoms.ring_offsets);
+      sj.vertex_offsets = reinterpret_cast<const unsigned long long*>(jb.geoms.vertex_offsets);
+      sj.xy = reinterpret_cast<const double2*>(jb.geoms.xy);
+      sj.values = b.per_geom_values ? jb.values : nullptr;
+    } else {
+      const size_t* o = &h_arr[6 * j];
+      sj.part_offsets = reinterpret_cast<const unsigned long long*>(ds + o[0]);
+      sj.part_kind = ds + o[1];
+      sj.ring_offsets = reinterpret_cast<const unsigned long long*>(ds + o[2]);
+      sj.vertex_offsets = reinterpret_cast<const unsigned long long*>(ds + o[3]);
+      sj.xy = reinterpret_cast<const double2*>(ds + o[4]);
+      sj.values = b.per_geom_values ? static_cast<const void*>(ds + o[5]) : nullptr;
+    }
+    dims[j] = job_dims(b.nrows, b.ncols, &jb.info, b.fn, touched, false, (unsigned)(bucket0[j] * WPT),
+                       base[(size_t)BK_GEOM * (n + 1) + j]);
+    fj[j].bucket0 = bucket0[j];
+    fj[j].out = out_dev ? jb.out : static_cast<void*>(static_cast<char*>(ctx->out.p) + out_off[j]);
+    fj[j].ncols = (int)b.ncols;
+    fj[j].ntx = (unsigned)b.ntx;
+  }
+  if (!in_dev) {
+    // pack the jobs' host arrays (large copies split over host threads)
+    auto pack = [&](unsigned j) {
+      const BatchJob& b = wave[j];
+      const rz_geoms& g = jobs[b.idx].geoms;
+      const size_t* o = &h_arr[6 * j];
+      std::memcpy(hs + o[0], g.part_offsets, 8 * (b.G + 1));
+      if (b.P) std::memcpy(hs + o[1], g.part_kind, b.P);
+      std::memcpy(hs + o[2], g.ring_offsets, 8 * (b.P + 1));
+      std::memcpy(hs + o[3], g.vertex_offsets, 8 * (b.R + 1));
+      if (b.V) std::memcpy(hs + o[4], g.xy, 16 * b.V);
+      if (b.per_geom_values && b.G) std::memcpy(hs + o[5], jobs[b.idx].values, tsize * b.G);
+    };
+    const unsigned nthreads = stage_bytes > (64u << 20) ? std::min(8u, n) : 1u;
+    if (nthreads > 1) {
+      std::vector<std::thread> ts;
+      for (unsigned t = 0; t < nthreads; ++t)
+        ts.emplace_back([&, t] {
+          for (unsigned j = t; j < n; j += nthreads) pack(j);
+        });
+      for (auto& t : ts) t.join();
+    } else {
+      for (unsigned j = 0; j < n; ++j) pack(j);
+    }
+  }
+  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[0], s));
+  RZ_CUDA(cudaMemcpyAsync(ds, hs, in_dev ? tables_bytes : stage_bytes, cudaMemcpyHostToDevice, s));
+  const JobSrc* d_src = reinterpret_cast<const JobSrc*>(ds + h_src);
+  const JobDims* d_dims = reinterpret_cast<const JobDims*>(ds + h_dims);
+  const FillJob* d_fj = reinterpret_cast<const FillJob*>(ds + h_fj);
+  const unsigned long long* d_base = reinterpret_cast<const unsigned long long*>(ds + h_base);
+
+  // ---- gather the wave's table ----
+  Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
+  int launches = 0;
+  RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
+  if (in_dev) {
+    k_batch_check<<<grid_for(n, 128, sms * 4), 128, 0, s>>>(d_src, n, d_ctrl);
+    ++launches;
+  }
+  unsigned long long* w_po = static_cast<unsigned long long*>(at(o_po));
+  unsigned char* w_pk = static_cast<unsigned char*>(at(o_pk));
+  unsigned long long* w_ro = static_cast<unsigned long long*>(at(o_ro));
+  unsigned long long* w_vo = static_cast<unsigned long long*>(at(o_vo));
+  double2* w_xy = static_cast<double2*>(at(o_xy));
+  void* w_val = at(o_val);
+  {
+    const unsigned gg = grid_for(Gt + 1, 256, sms * 16);
+    switch (tsize) {
+      case 1: k_batch_geoms<1><<<gg, 256, 0, s>>>(d_src, d_base, n, w_po, w_val); break;
+      case 2: k_batch_geoms<2><<<gg, 256, 0, s>>>(d_src, d_base, n, w_po, w_val); break;
+      case 4: k_batch_geoms<4><<<gg, 256, 0, s>>>(d_src, d_base, n, w_po, w_val); break;
+      default: k_batch_geoms<8><<<gg, 256, 0, s>>>(d_src, d_base, n, w_po, w_val); break;
+    }
+    k_batch_parts<<<grid_for(Pt + 1, 256, sms * 16), 256, 0, s>>>(d_src, d_base, n, w_pk, w_ro);
+    k_batch_rings<<<grid_for(Rt + 1, 256, sms * 16), 256, 0, s>>>(d_src, d_base, n, w_vo,
+                                                                   static_cast<unsigned char*>(at(o_rc)));
+    k_batch_vertices<<<grid_for(Vt + 1, 256, sms * 16), 256, 0, s>>>(d_src, d_base, n, w_xy);
+    launches += 4;
+  }
+  Geo geo;
+  geo.n_geoms = Gt;
+  geo.n_parts = Pt;
+  geo.n_rings = Rt;
+  geo.n_vertices = Vt;
+  geo.part_offsets = w_po;
+  geo.part_kind = w_pk;
+  geo.ring_offsets = w_ro;
+  geo.vertex_offsets = w_vo;
+  geo.xy = w_xy;
+  geo.bands = nullptr;
+  geo.ring_closed = static_cast<const unsigned char*>(at(o_rc));
+
+  // ---- prep ----
+  PartTables pt;
+  pt.part_geom = static_cast<unsigned*>(at(o_pg));
+  pt.plan = static_cast<PartPlan*>(at(o_plan));
+  pt.counts = static_cast<unsigned long long*>(at(o_cnt));
+  pt.poff = static_cast<unsigned long long*>(at(o_poff));
+  pt.tmp64 = static_cast<unsigned long long*>(at(o_tmp64));
+  pt.line_parts = static_cast<unsigned*>(at(o_lp));
+  pt.point_parts = static_cast<unsigned*>(at(o_pp));
+  pt.last_kept = static_cast<unsigned long long*>(at(o_last));
+  launches += launch_prep(geo, ident, dims[0], d_dims, n, 0u, pt, d_ctrl, sms, s);
+  RZ_CUDA(cudaMemsetAsync(pt.last_kept, 0, 8 * (Pt ? Pt : 1), s));
+  unsigned* bcount = static_cast<unsigned*>(at(o_bc));
+  unsigned* boff = static_cast<unsigned*>(at(o_boff));
+  unsigned* big = static_cast<unsigned*>(at(o_big));
+  unsigned char* gctr = static_cast<unsigned char*>(at(o_gctr));
+  const fill_fn fill = fill_for(dt);
+
+  unsigned long long cap = std::max<unsigned long long>(ctx->span_cap_hint, 2 * Vt + (1ull << 20));
+  if (cap > 0xFFFFFFF0ull) cap = 0xFFFFFFF0ull;
+  unsigned reruns = 0;
+  while (true) {
+    cap &= ~1ull;
+    RZ_CUDA(ensure(ctx->spans, RECORD_BYTES * cap + 16));
+    cap = std::min<unsigned long long>(cap, (ctx->spans.cap - 16) / RECORD_BYTES) & ~1ull;
+    RecBuf sb;
+    sb.cap = cap;
+    sb.wid = static_cast<unsigned*>(ctx->spans.p);
+    sb.part = sb.wid + cap;
+    sb.mask = sb.part + cap;
+    uint2* sorted = reinterpret_cast<uint2*>(sb.mask + cap);
+    void* rvals = sorted + cap;
+    k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
+    RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * (nbuckets ? nbuckets : 1), s));
+    RZ_CUDA(cudaMemsetAsync(gctr, 0, 16 * (n + 1), s));
+    ++launches;
+    launches += launch_coverage(geo, ident, pt, sb, bcount, d_ctrl, sms, ctx->narrow_blocks_per_sm,
+                                ctx->poly_blocks_per_sm, s);
+    if (nbuckets) {
+      launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
+      launch_scatter(tsize, sms, s, sb, boff, bcount, sorted, w_val, pt.part_geom, rvals, d_ctrl);
+      ++launches;
+      // one fill per variant: a run of jobs with equal (fn, dedup, background)
+      unsigned g = 0;
+      for (unsigned j0 = 0; j0 < n; ++g) {
+        unsigned j1 = j0 + 1;
+        while (j1 < n && wave[j1].fn == wave[j0].fn && wave[j1].dedup == wave[j0].dedup &&
+               wave[j1].bg_bits == wave[j0].bg_bits)
+          ++j1;
+        const unsigned long long lo = bucket0[j0], hi = bucket0[j1];
+        if (hi > lo) {
+          FillArgs fa;
+          fa.offsets = boff + lo;
+          fa.recs = sorted;
+          fa.rvals = rvals;
+          fa.nbuckets = hi - lo;
+          fa.scalar = 0;
+          fa.out = nullptr;
+          set_background(fa, wave[j0].bg_bits, tsize);
+          fa.nrows = fa.ncols = 0;
+          fa.ntx = 1;
+          fa.big = big + lo;
+          fa.ctrl = d_ctrl;
+          fa.rec_cap = cap;
+          fa.work = reinterpret_cast<unsigned long long*>(gctr + 16 * g);
+          fa.nbig = reinterpret_cast<unsigned*>(gctr + 16 * g + 8);
+          fa.jobs = d_fj;
+          fa.n_jobs = n;
+          fa.bucket0 = lo;
+          launches += fill(fa, (int)wave[j0].fn, wave[j0].dedup, sms, s);
+        }
+        j0 = j1;
+      }
+    }
+    RZ_CUDA(cudaGetLastError());
+    RZ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+    RZ_CUDA(cudaStreamSynchronize(s));
+    Ctrl& hc = *ctx->h_ctrl;
+    if (hc.err == ERR_BAD_JOB && hc.err_index < n) hc.err_index = wave[hc.err_index].idx;  // the caller's index
+    if (hc.err) return ctrl_error(hc, err, errlen);
+    if (hc.span_count > cap) {
+      unsigned long long want = hc.span_count + hc.span_count / 4 + 1024;
+      if (want > 0xFFFFFFF0ull) {
+        if (hc.span_count > 0xFFFFFFF0ull)
+          return fail(err, errlen, RZ_VALUE_ERROR, "more than 2^32 coverage records in one wave");
+        want = 0xFFFFFFF0ull;
+      }
+      cap = want;
+      ctx->span_cap_hint = cap;
+      ++reruns;
+      continue;
+    }
+    if (stats) {
+      stats->edges += hc.edges;
+      stats->records += hc.span_count;
+      stats->pixel_writes += hc.pixel_writes;
+    }
+    break;
+  }
+  if (!out_dev) {
+    for (unsigned j = 0; j < n; ++j) {
+      const BatchJob& b = wave[j];
+      if (b.out_elems)
+        RZ_CUDA(cudaMemcpyAsync(jobs[b.idx].out, static_cast<char*>(ctx->out.p) + out_off[j], b.out_elems * tsize,
+                                cudaMemcpyDeviceToHost, s));
+    }
+  }
+  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[6], s));
+  RZ_CUDA(cudaStreamSynchronize(s));
+  if (stats) {
+    stats->waves += 1;
+    stats->kernel_launches += (uint32_t)launches;
+    stats->reruns += reruns;
+    if (timing) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[6]);
+      stats->ms_device_total += ms;
+    }
+  }
+  return RZ_OK;
+}
+
+}  // namespace
+
+extern "C" rz_status rz_rasterize_batch(rz_context* ctx, const rz_job* jobs, size_t n_jobs, rz_dtype dt,
+                                        uint32_t flags, uint64_t wave_bytes, rz_batch_stats* stats, char* err,
+                                        size_t errlen) {
+  using clk = std::chrono::steady_clock;
+  const auto t_host0 = clk::now();
+  rz::clear_err(err, errlen);
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (!ctx || (n_jobs && !jobs)) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null argument");
+  const size_t tsize = rz_dtype_size(dt);
+  if (tsize == 0) return fail(err, errlen, RZ_VALUE_ERROR, "Unsupported dtype");
+  const bool in_dev = flags & RZ_FLAG_INPUT_DEVICE, out_dev = flags & RZ_FLAG_OUTPUT_DEVICE;
+  if (!wave_bytes) wave_bytes = 8ull << 30;
+  // ---- validate every job before any work ----
+  std::vector<BatchJob> all(n_jobs);
+  unsigned long long total_out = 0;
+  for (size_t i = 0; i < n_jobs; ++i) {
+    const rz_job& jb = jobs[i];
+    const rz_geoms& g = jb.geoms;
+    BatchJob& b = all[i];
+    b.idx = i;
+    b.G = g.n_geoms;
+    b.P = g.n_parts;
+    b.R = g.n_rings;
+    b.V = g.n_vertices;
+    if ((int)jb.fn < 0 || (int)jb.fn > 6)
+      return fail(err, errlen, RZ_VALUE_ERROR, "job %zu: Unknown pixel function", i);
+    if (!jb.background) return fail(err, errlen, RZ_INVALID_ARGUMENT, "job %zu: null background", i);
+    if (jb.info.nrows >= (1ull << 31) - 1 || jb.info.ncols >= (1ull << 31) - 1)
+      return fail(err, errlen, RZ_VALUE_ERROR, "job %zu: raster dimensions must be below 2^31-1", i);
+    if (b.G >= 0xFFFFFFFFull || b.P >= (1ull << 27))
+      return fail(err, errlen, RZ_VALUE_ERROR, "job %zu: at most 2^32-1 geometries and 2^27 parts are supported", i);
+    if (!g.part_offsets || !g.ring_offsets || !g.vertex_offsets || (b.P && !g.part_kind) || (b.V && !g.xy))
+      return fail(err, errlen, RZ_INVALID_ARGUMENT, "job %zu: geometry table has null arrays", i);
+    if (in_dev && (reinterpret_cast<uintptr_t>(g.xy) & 15))
+      return fail(err, errlen, RZ_INVALID_ARGUMENT, "job %zu: device xy must be 16-byte aligned", i);
+    if (!in_dev && (g.part_offsets[0] != 0 || g.part_offsets[b.G] != b.P || g.ring_offsets[0] != 0 ||
+                    g.ring_offsets[b.P] != b.R || g.vertex_offsets[0] != 0 || g.vertex_offsets[b.R] != b.V))
+      return fail(err, errlen, RZ_INVALID_ARGUMENT, "job %zu: geometry table sizes are inconsistent", i);
+    b.nrows = jb.info.nrows;
+    b.ncols = jb.info.ncols;
+    b.ntx = (b.ncols + TW - 1) >> TW_SHIFT;
+    b.out_elems = b.nrows * b.ncols;
+    b.buckets = b.nrows * b.ntx;
+    if (b.buckets >= (1ull << 28))
+      return fail(err, errlen, RZ_VALUE_ERROR, "job %zu: raster too large: more than 2^28 (row,tile) buckets", i);
+    if (b.out_elems && !jb.out) return fail(err, errlen, RZ_INVALID_ARGUMENT, "job %zu: null output", i);
+    b.fn = jb.fn;
+    b.dedup = fill_dedup(&jb.info, jb.fn, flags & RZ_FLAG_ALL_TOUCHED);
+    b.bg_bits = 0;
+    std::memcpy(&b.bg_bits, jb.background, tsize);
+    b.per_geom_values = jb.values && !(jb.flags & RZ_FLAG_SCALAR_VALUE);
+    b.scalar_bits = one_bits(dt);
+    if (jb.values && (jb.flags & RZ_FLAG_SCALAR_VALUE)) {
+      b.scalar_bits = 0;
+      std::memcpy(&b.scalar_bits, jb.values, tsize);
+    }
+    const size_t geo_bytes = 8 * (b.G + 1) + b.P + 8 * (b.P + 1) + 8 * (b.R + 1) + 16 * b.V + tsize * b.G;
+    b.dev_bytes = (out_dev ? 0 : b.out_elems * tsize) + geo_bytes * (in_dev ? 1 : 2) +
+                  b.P * (4 + sizeof(PartPlan) + 16 * PC_N + 16) + 16 * b.buckets;
+    total_out += b.out_elems * tsize;
+  }
+  if (stats) {
+    stats->jobs = n_jobs;
+    stats->out_bytes = total_out;
+  }
+  if (!n_jobs) return RZ_OK;
+  RZ_CUDA(cudaSetDevice(ctx->device));
+  // ---- waves, in caller order ----
+  std::vector<BatchJob> wave;
+  size_t bytes = 0;
+  unsigned long long G = 0, P = 0, buckets = 0;
+  auto flush = [&]() -> rz_status {
+    if (wave.empty()) return RZ_OK;
+    const rz_status st = run_wave(ctx, jobs, wave, dt, flags, stats, err, errlen);
+    wave.clear();
+    bytes = 0;
+    G = P = buckets = 0;
+    return st;
+  };
+  for (size_t i = 0; i < n_jobs; ++i) {
+    const BatchJob& b = all[i];
+    if (!wave.empty() && (bytes + b.dev_bytes > wave_bytes || G + b.G >= 0xFFFFFFFFull ||
+                          P + b.P >= (1ull << 27) || buckets + b.buckets >= (1ull << 28) || wave.size() >= 65536)) {
+      const rz_status st = flush();
+      if (st != RZ_OK) return st;
+    }
+    wave.push_back(b);
+    bytes += b.dev_bytes;
+    G += b.G;
+    P += b.P;
+    buckets += b.buckets;
+  }
+  const rz_status st = flush();
+  if (st != RZ_OK) return st;
+  if (stats) stats->ms_host_total = std::chrono::duration<float, std::milli>(clk::now() - t_host0).count();
   return RZ_OK;
 }

@@ -14,6 +14,15 @@
 
 namespace rzd {
 
+// One job of a batch call, as the fill sees it: where its buckets start and
+// where its raster goes.
+struct FillJob {
+  unsigned long long bucket0;  // first bucket of the job (in the call's numbering)
+  void* out;                   // (nrows, ncols) raster of the job
+  int ncols;
+  unsigned ntx;
+};
+
 struct FillArgs {
   const unsigned* offsets;  // [nbuckets + 1]
   const uint2* recs;        // {part | word << REC_W_SHIFT | DEDUP_BIT, mask} grouped by bucket
@@ -28,7 +37,45 @@ struct FillArgs {
   unsigned* big;            // buckets left to the per-word kernel
   Ctrl* ctrl;
   unsigned long long rec_cap;
+  unsigned long long* work;  // chunk counter of this fill (zero before the launch)
+  unsigned* nbig;            // entries of `big` (zero before the launch)
+  // batch calls: bucket b of this fill is bucket bucket0 + b of the call, and
+  // its raster is that of the job owning it; jobs == nullptr: out / ncols / ntx
+  const FillJob* jobs;
+  unsigned n_jobs;
+  unsigned long long bucket0;
 };
+
+// The raster tile of bucket b: its first pixel and its width (the last tile
+// of a row is cut at ncols).
+template <typename T>
+__device__ __forceinline__ T* bucket_tile(const FillArgs& a, unsigned long long b, int& len) {
+  T* out;
+  int ncols;
+  unsigned ntx, lb;
+  if (a.jobs) {
+    const unsigned long long gb = a.bucket0 + b;
+    unsigned lo = 0, hi = a.n_jobs;  // jobs[lo].bucket0 <= gb < jobs[hi].bucket0
+    while (hi - lo > 1) {
+      const unsigned mid = (lo + hi) >> 1;
+      if (a.jobs[mid].bucket0 <= gb) lo = mid; else hi = mid;
+    }
+    const FillJob j = a.jobs[lo];
+    out = static_cast<T*>(j.out);
+    ncols = j.ncols;
+    ntx = j.ntx;
+    lb = (unsigned)(gb - j.bucket0);
+  } else {
+    out = static_cast<T*>(a.out);
+    ncols = a.ncols;
+    ntx = a.ntx;
+    lb = (unsigned)b;
+  }
+  const unsigned rowid = lb / ntx;  // 32-bit: a 64-bit divide runs on the FP64 pipe
+  const int c0 = (int)(lb - rowid * ntx) << TW_SHIFT;
+  len = min(TW, ncols - c0);
+  return out + (unsigned long long)rowid * (unsigned long long)ncols + c0;
+}
 
 template <typename T> __device__ __forceinline__ bool is_nan_v(T v) { return false; }
 template <> __device__ __forceinline__ bool is_nan_v<float>(float v) { return isnan(v); }
@@ -380,11 +427,10 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
   SRec* srec = reinterpret_cast<SRec*>(smem + warp * fill_warp_bytes<T>());
   const T bg = from_bits<T>(a.bg);
   const BgF64 bgc = bg_f64(a.bg);
-  T* out = static_cast<T*>(a.out);
   const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
   while (true) {
     unsigned long long ch = 0;
-    if (lane == 0) ch = atomicAdd(&a.ctrl->fill_work, 1ull);
+    if (lane == 0) ch = atomicAdd(a.work, 1ull);
     ch = __shfl_sync(0xFFFFFFFFu, ch, 0);
     if (ch >= nchunks) break;
     const unsigned long long b0 = ch * FILL_CHUNK;
@@ -404,17 +450,15 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
         n_next = (int)((k + 2 < nb ? __shfl_sync(0xFFFFFFFFu, off, (k + 2) & 31) : off_end) - o_next);
         nxt = load_pair<T>(a, o_next, n_next);
       }
-      const unsigned rowid = (unsigned)b / a.ntx;  // 32-bit: a 64-bit divide runs on the FP64 pipe
-      const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
-      const int len = min(TW, a.ncols - c0);
-      T* dst = out + (unsigned long long)rowid * (unsigned long long)a.ncols + c0;
+      int len;
+      T* dst = bucket_tile<T>(a, b, len);
       if (n == 0) {
         store_bg<T>(dst, len, a.bg16, bg, lane, 32);
         continue;
       }
       if (n > FILL_WARP_MAX) {
         if (n > FILL_WARP_SORT) {
-          if (lane == 0) a.big[atomicAdd(&a.ctrl->big_count, 1u)] = (unsigned)b;
+          if (lane == 0) a.big[atomicAdd(a.nbig, 1u)] = (unsigned)b;
           continue;
         }
         // up to FILL_WARP_SORT records: staged and sorted in shared memory,
@@ -572,17 +616,16 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
   unsigned* hist = reinterpret_cast<unsigned*>(wbase + BIG_CAP * 8 + BIG_CAP * sizeof(T));
   const T bg = from_bits<T>(a.bg);
   const BgF64 bgc = bg_f64(a.bg);
-  T* out = static_cast<T*>(a.out);
-  const unsigned long long items = (unsigned long long)ctrl->big_count * WPT;
+  const unsigned long long items = (unsigned long long)*a.nbig * WPT;
   const unsigned long long nwarps = (unsigned long long)gridDim.x * BIG_WARPS;
   for (unsigned long long it = (unsigned long long)blockIdx.x * BIG_WARPS + warp; it < items; it += nwarps) {
     const unsigned long long b = a.big[it / WPT];
     const unsigned wsel = (unsigned)(it % WPT);
     const unsigned o0 = a.offsets[b];
     const int n = (int)(a.offsets[b + 1] - o0);
-    const unsigned rowid = (unsigned)b / a.ntx;
-    const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
-    const int x = c0 + (int)wsel * 32 + lane;
+    int len;
+    T* dst = bucket_tile<T>(a, b, len);
+    const int x = (int)wsel * 32 + lane;
     T c = bg;
     unsigned last_part = 0xFFFFFFFFu;
     unsigned lo_part = 0;  // parts < lo_part are done
@@ -675,7 +718,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
       __syncwarp();
       lo_part = hi;
     }
-    if (x < a.ncols) out[(unsigned long long)rowid * (unsigned long long)a.ncols + x] = c;
+    if (x < len) dst[x] = c;
   }
 }
 
@@ -695,11 +738,10 @@ __global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const T bg = from_bits<T>(a.bg);
-  T* out = static_cast<T*>(a.out);
   const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
   while (true) {
     unsigned long long ch = 0;
-    if (lane == 0) ch = atomicAdd(&a.ctrl->fill_work, 1ull);
+    if (lane == 0) ch = atomicAdd(a.work, 1ull);
     ch = __shfl_sync(0xFFFFFFFFu, ch, 0);
     if (ch >= nchunks) break;
     const unsigned long long b0 = ch * FILL_CHUNK;
@@ -719,10 +761,8 @@ __global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
         e_next = k + 2 < nb ? __shfl_sync(0xFFFFFFFFu, off, (k + 2) & 31) : off_end;
         nxt = lane < (int)(e_next - o_next) ? a.recs[o_next + lane] : make_uint2(0u, 0u);
       }
-      const unsigned rowid = (unsigned)b / a.ntx;
-      const int c0 = (int)((unsigned)b - rowid * a.ntx) << TW_SHIFT;
-      const int len = min(TW, a.ncols - c0);
-      T* dst = out + (unsigned long long)rowid * (unsigned long long)a.ncols + c0;
+      int len;
+      T* dst = bucket_tile<T>(a, b, len);
       if (n == 0) {
         store_bg<T>(dst, len, a.bg16, bg, lane, 32);
         continue;

@@ -66,8 +66,9 @@ __global__ void k_part_geom(Geo geo, unsigned* part_geom, Ctrl* ctrl) {
 // geometry from the min/max of their world coordinates (the world->pixel
 // map is monotone, so transforming the extremes gives the pixel extremes);
 // line and point parts just report their vertex counts.
-__global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan* plan,
-                            unsigned long long* counts /*[P][PC_N]*/, Ctrl* ctrl) {
+__global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restrict__ jobs, unsigned n_jobs,
+                            const unsigned* part_geom, PartPlan* plan, unsigned long long* counts /*[P][PC_N]*/,
+                            Ctrl* ctrl) {
   if (ctrl->err) return;
   const int lane = threadIdx.x & 31;
   const unsigned long long warp0 = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
@@ -77,9 +78,19 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
     const unsigned kind = geo.part_kind[p];
     const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
     const unsigned long long vs = geo.vertex_offsets[rb], ve = geo.vertex_offsets[re];
-    const unsigned band = geo.bands ? geo.bands[part_geom[p]] : 0u;
+    const unsigned gi = part_geom[p];
+    const unsigned band = geo.bands ? geo.bands[gi] : 0u;
+    const JobDims jd = jobs ? jobs[job_of(jobs, n_jobs, gi)] : one;
     unsigned long long c[PC_N] = {0, 0, 0, 0, 0, 0};
-    PartPlan pl = {0, 0, 0, 0, 0, band};
+    PartPlan pl;
+    pl.row0 = pl.row1 = pl.col0 = pl.bw = pl.wr = 0;
+    pl.band = band;
+    pl.nrows = jd.nrows;
+    pl.ncols = jd.ncols;
+    pl.wpr = jd.ntx * WPT;
+    pl.wid0 = jd.wid_base + band * (unsigned)jd.nrows * pl.wpr;
+    pl.flags = kind == 1 ? jd.line_flag : (kind == 2 ? jd.poly_flag : 0u);
+    pl.pad = 0;
     if (kind != 0) {
       // segments = vertices - non-empty rings
       unsigned long long nonempty = 0;
@@ -131,10 +142,10 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
       };
       if (ylo <= yhi) {
         // pixel y decreases with world y
-        const int row0 = row_ceil(to_py(g, unkey(yhi)), g.nrows);
-        const int row1 = row_ceil(to_py(g, unkey(ylo)), g.nrows);
+        const int row0 = row_ceil(to_py(g, unkey(yhi)), jd.nrows);
+        const int row1 = row_ceil(to_py(g, unkey(ylo)), jd.nrows);
         if (row1 > row0) {
-          double c_lo = 0.0, c_hi = (double)g.ncols;
+          double c_lo = 0.0, c_hi = (double)jd.ncols;
           if (xlo <= xhi && !nan_x) {
             const double pxl = to_px(g, unkey(xlo)), pxh = to_px(g, unkey(xhi));
             // crossings are interpolations between edge end points; allow a
@@ -145,8 +156,8 @@ __global__ void k_part_prep(Geo geo, Grid g, const unsigned* part_geom, PartPlan
             c_hi = ceil(pxh + margin);
           }
           // the bitmap starts on a 32-pixel word so that its words are raster words
-          const int col0 = (c_lo <= 0.0 ? 0 : (c_lo >= g.ncols ? g.ncols : (int)c_lo)) & ~31;
-          const int colmax = c_hi <= 0.0 ? 0 : (c_hi >= g.ncols ? g.ncols : (int)c_hi);
+          const int col0 = (c_lo <= 0.0 ? 0 : (c_lo >= jd.ncols ? jd.ncols : (int)c_lo)) & ~31;
+          const int colmax = c_hi <= 0.0 ? 0 : (c_hi >= jd.ncols ? jd.ncols : (int)c_hi);
           const int bw = (colmax - col0 + 1 + 31) >> 5;
           const bool narrow = bw <= SMALL_BW;
           int wr = (narrow ? SMALL_BITMAP_WORDS : BITMAP_WORDS) / bw;
@@ -226,21 +237,19 @@ struct RunEmitter {
 };
 
 __device__ __forceinline__ void run_flush(RunEmitter& re, const RecBuf& sb, unsigned* bucket_count,
-                                          Ctrl* ctrl, const Grid& g, unsigned band, unsigned part,
-                                          unsigned flags) {
+                                          Ctrl* ctrl, const PartPlan& pl, unsigned part) {
   if (re.y >= 0) {
     re.npix += (unsigned long long)(re.xb - re.xa);
-    emit_run(sb, bucket_count, ctrl, g, band, re.y, re.xa, re.xb, part | flags);
+    emit_run(sb, bucket_count, ctrl, pl, re.y, re.xa, re.xb, part | pl.flags);
   }
   re.y = -1;
 }
 
 __device__ __forceinline__ void run_add(RunEmitter& re, const RecBuf& sb, unsigned* bucket_count, Ctrl* ctrl,
-                                        const Grid& g, unsigned band, unsigned part, unsigned flags, int y,
-                                        int x) {
+                                        const PartPlan& pl, unsigned part, int y, int x) {
   if (re.y == y && x == re.xb) { re.xb = x + 1; return; }
   if (re.y == y && x == re.xa - 1) { re.xa = x; return; }
-  run_flush(re, sb, bucket_count, ctrl, g, band, part, flags);
+  run_flush(re, sb, bucket_count, ctrl, pl, part);
   re.y = y;
   re.xa = x;
   re.xb = x + 1;
@@ -254,10 +263,10 @@ __device__ __forceinline__ void run_add(RunEmitter& re, const RecBuf& sb, unsign
 // after which the caller reports an error.
 template <typename Emit>
 __device__ __forceinline__ bool all_touched_walk(double df_x, double df_y, double df_x_end, double df_y_end,
-                                                 const Grid& g, Emit&& emit) {
+                                                 int nrows_i, int ncols_i, Emit&& emit) {
   const double EPSILON_INTERSECT = 1e-4, TOLERANCE = 1e-9;
-  const long long nrows = g.nrows, ncols = g.ncols;
-  const double nrows_f = (double)g.nrows, ncols_f = (double)g.ncols;
+  const long long nrows = nrows_i, ncols = ncols_i;
+  const double nrows_f = (double)nrows_i, ncols_f = (double)ncols_i;
   if (df_x > df_x_end) {  // proceed left to right
     double t = df_x; df_x = df_x_end; df_x_end = t;
     t = df_y; df_y = df_y_end; df_y_end = t;
@@ -338,8 +347,7 @@ __device__ __forceinline__ bool all_touched_walk(double df_x, double df_y, doubl
 // part's last kept segment is written by k_line_endpix.
 __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
                              const unsigned long long* __restrict__ poff, const unsigned* __restrict__ line_parts,
-                             unsigned long long* last_kept, unsigned dedup_flag, RecBuf sb,
-                             unsigned* bucket_count, Ctrl* ctrl) {
+                             unsigned long long* last_kept, RecBuf sb, unsigned* bucket_count, Ctrl* ctrl) {
   if (ctrl->err) return;
   const unsigned long long nlist = poff[geo.n_parts * PC_N + PC_LINE_P];
   const unsigned long long total = poff[geo.n_parts * PC_N + PC_LINE_V];
@@ -360,16 +368,16 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
     const double x1 = to_px(g, w1.x), y1 = to_py(g, w1.y);
     const double min_x = min_rs(x0, x1), max_x = max_rs(x0, x1);
     const double min_y = min_rs(y0, y1), max_y = max_rs(y0, y1);
-    if (!(min_x < (double)g.ncols && max_x >= 0.0 && min_y < (double)g.nrows && max_y >= 0.0)) continue;
-    const unsigned band = plan[p].band;
+    const PartPlan pl = plan[p];
+    if (!(min_x < (double)pl.ncols && max_x >= 0.0 && min_y < (double)pl.nrows && max_y >= 0.0)) continue;
     if (g.touched) {  // AllTouched::burn_line; polygon rings too (burn_geometry.rs:88-100, 226-238)
-      // a polygon's ring walk shares the polygon's PixelCache (sum / count
-      // only); the non-square-pixel cache of LineString::burn is not its
-      const unsigned flag = geo.part_kind[p] == 2 ? g.poly_flags : dedup_flag;
-      const bool ok = all_touched_walk(x0, y0, x1, y1, g, [&](int yy, int xx) {
-        run_add(run, sb, bucket_count, ctrl, g, band, p, flag, yy, xx);
+      // a polygon's ring walk carries the polygon's flags: it shares the
+      // polygon's PixelCache (sum / count only), not the non-square-pixel
+      // cache of LineString::burn
+      const bool ok = all_touched_walk(x0, y0, x1, y1, pl.nrows, pl.ncols, [&](int yy, int xx) {
+        run_add(run, sb, bucket_count, ctrl, pl, p, yy, xx);
       });
-      run_flush(run, sb, bucket_count, ctrl, g, band, p, flag);
+      run_flush(run, sb, bucket_count, ctrl, pl, p);
       if (!ok) set_error(ctrl, ERR_LINE_LONG, v);
       continue;
     }
@@ -388,13 +396,13 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
     const long long sx = ix0 < ix1 ? 1 : -1, sy = iy0 < iy1 ? 1 : -1;
     long long err = dx + dy;
     while (ix0 != ix1 || iy0 != iy1) {
-      if (ix0 >= 0 && ix0 < g.ncols && iy0 >= 0 && iy0 < g.nrows)
-        run_add(run, sb, bucket_count, ctrl, g, band, p, dedup_flag, (int)iy0, (int)ix0);
+      if (ix0 >= 0 && ix0 < pl.ncols && iy0 >= 0 && iy0 < pl.nrows)
+        run_add(run, sb, bucket_count, ctrl, pl, p, (int)iy0, (int)ix0);
       const long long e2 = 2 * err;
       if (e2 >= dy) { err += dy; ix0 += sx; }
       if (e2 <= dx) { err += dx; iy0 += sy; }
     }
-    run_flush(run, sb, bucket_count, ctrl, g, band, p, dedup_flag);
+    run_flush(run, sb, bucket_count, ctrl, pl, p);
   }
   unsigned long long npix = run.npix;
   for (int o = 16; o > 0; o >>= 1) npix += __shfl_xor_sync(0xFFFFFFFFu, npix, o);
@@ -405,7 +413,7 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
 // is written unless that segment's linestring is closed.
 __global__ void k_line_endpix(Geo geo, Grid g, const PartPlan* __restrict__ plan,
                               const unsigned long long* __restrict__ poff, const unsigned* __restrict__ line_parts,
-                              const unsigned long long* __restrict__ last_kept, unsigned dedup_flag, RecBuf sb,
+                              const unsigned long long* __restrict__ last_kept, RecBuf sb,
                               unsigned* bucket_count, Ctrl* ctrl) {
   if (ctrl->err) return;
   const unsigned long long nlist = poff[geo.n_parts * PC_N + PC_LINE_P];
@@ -417,14 +425,19 @@ __global__ void k_line_endpix(Geo geo, Grid g, const PartPlan* __restrict__ plan
     const unsigned long long v = last_kept[p] - 1;
     const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
     const unsigned long long r = ring_of(geo, rb, re, v);
-    const double2 first = geo.xy[geo.vertex_offsets[r]];
-    const double2 last = geo.xy[geo.vertex_offsets[r + 1] - 1];
-    if (first.x == last.x && first.y == last.y) continue;  // LineString::is_closed
+    if (geo.ring_closed) {
+      if (geo.ring_closed[r]) continue;
+    } else {
+      const double2 first = geo.xy[geo.vertex_offsets[r]];
+      const double2 last = geo.xy[geo.vertex_offsets[r + 1] - 1];
+      if (first.x == last.x && first.y == last.y) continue;  // LineString::is_closed
+    }
     const double2 w1 = geo.xy[v + 1];
     const long long ix = as_isize(floor(to_px(g, w1.x))), iy = as_isize(floor(to_py(g, w1.y)));
-    if (ix >= 0 && ix < g.ncols && iy >= 0 && iy < g.nrows) {
+    const PartPlan pl = plan[p];
+    if (ix >= 0 && ix < pl.ncols && iy >= 0 && iy < pl.nrows) {
       ++npix;
-      emit_run(sb, bucket_count, ctrl, g, plan[p].band, (int)iy, (int)ix, (int)ix + 1, p | dedup_flag);
+      emit_run(sb, bucket_count, ctrl, pl, (int)iy, (int)ix, (int)ix + 1, p | pl.flags);
     }
   }
   if (npix) atomicAdd(&ctrl->pixel_writes, npix);
@@ -450,9 +463,10 @@ __global__ void k_point_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan
         geo.vertex_offsets[geo.ring_offsets[p]] + (t - poff[(unsigned long long)p * PC_N + PC_POINT_V]);
     const double2 w = geo.xy[v];
     const double x = to_px(g, w.x), y = to_py(g, w.y);
-    if (x >= 0.0 && x < (double)g.ncols && y >= 0.0 && y < (double)g.nrows) {
+    const PartPlan pl = plan[p];
+    if (x >= 0.0 && x < (double)pl.ncols && y >= 0.0 && y < (double)pl.nrows) {
       ++npix;
-      emit_run(sb, bucket_count, ctrl, g, plan[p].band, (int)y, (int)x, (int)x + 1, p);
+      emit_run(sb, bucket_count, ctrl, pl, (int)y, (int)x, (int)x + 1, p);
     }
   }
   for (int o = 16; o > 0; o >>= 1) npix += __shfl_xor_sync(0xFFFFFFFFu, npix, o);

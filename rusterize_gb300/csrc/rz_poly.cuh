@@ -60,6 +60,7 @@ constexpr int STAGE_CAP = (QCAP * 32) / 12 / 8 * 8;  // staged records per warp 
 
 struct PolyWin {
   int r0, r1, col0, nbits, bw;
+  int nrows, ncols;  // the part's raster
 };
 
 // Per-warp shared-memory scratch: the edge queue, which doubles as the
@@ -81,7 +82,8 @@ struct WarpScratch {
 // `row`, by the reference's FP64 sequence: PolyEdge::new's slope and
 // intersect_at (edges.rs:27-55), no FMA.  Used for the crossings the FP32
 // filter leaves undecided.  Returns the boundary, or -1 for a +NaN crossing.
-__device__ __noinline__ int cross_exact(const Geo& geo, const Grid& g, unsigned long long v, bool top0, int row) {
+__device__ __noinline__ int cross_exact(const Geo& geo, const Grid& g, unsigned long long v, bool top0, int row,
+                                        int ncols) {
   const double2 w0 = geo.xy[v], w1 = geo.xy[v + 1];
   const double px0 = to_px(g, w0.x), py0 = to_py(g, w0.y), px1 = to_px(g, w1.x), py1 = to_py(g, w1.y);
   const double xt = top0 ? px0 : px1, yt = top0 ? py0 : py1;
@@ -90,7 +92,7 @@ __device__ __noinline__ int cross_exact(const Geo& geo, const Grid& g, unsigned 
   const double x = __dadd_rn(xt, __dmul_rn(__dsub_rn(half_int(row), yt), dxdy));
   const unsigned long long xbits = f64_bits(x);
   if (nan_bits(xbits)) return (xbits >> 63) ? 0 : -1;  // -NaN sorts first; +NaN pairs into an empty span
-  return floor_half_up(x, g.ncols);                    // floor(x + 0.5) clamped, burners.rs:310-311
+  return floor_half_up(x, ncols);                      // floor(x + 0.5) clamped, burners.rs:310-311
 }
 
 // Crossings of the nq queued edges; MODE 0 toggles them in the bitmap, MODE 1
@@ -135,9 +137,9 @@ __device__ __forceinline__ void warp_cross(const Geo& geo, const Grid& g, const 
       ce.c0 = qe.c0;
       ce.e0 = qe.e0;
       ce.e1 = qe.e1;
-      int r = cross_fast(ce, j, g.ncols);
+      int r = cross_fast(ce, j, w.ncols);
       if (r < 0) {
-        r = cross_exact(geo, g, vs + (qe.v & 0x7FFFFFFFu), qe.v >> 31, row);
+        r = cross_exact(geo, g, vs + (qe.v & 0x7FFFFFFFu), qe.v >> 31, row, w.ncols);
         if (r < 0) continue;
       }
       const int loc = r - w.col0;
@@ -164,12 +166,12 @@ struct VtxState {
   bool ok;
 };
 
-__device__ __forceinline__ VtxState vtx_state(const Grid& g, double2 w) {
+__device__ __forceinline__ VtxState vtx_state(const Grid& g, double2 w, int nrows) {
   VtxState s;
   s.py = to_py(g, w.y);
   uint32_t yf24 = 0;
   const bool oky = rzb::split_px(s.py, s.yi, s.yf, &yf24);
-  s.ys = rzb::ceil_half_down_split(s.py, oky, s.yi, yf24, g.nrows);  // edges.rs:32-33
+  s.ys = rzb::ceil_half_down_split(s.py, oky, s.yi, yf24, nrows);  // edges.rs:32-33
   const double px = to_px(g, w.x);
   const bool okx = rzb::split_px(px, s.xi, s.xf);
   s.ok = okx && oky;
@@ -221,7 +223,7 @@ __device__ __forceinline__ void warp_pass(const Geo& geo, const Grid& g, unsigne
   carry.ys = carry.xi = carry.yi = 0;
   carry.xf = carry.yf = 0.0f;
   carry.ok = false;
-  if (vb > 0 && lane == 0) carry = vtx_state(g, xy[vb - 1]);
+  if (vb > 0 && lane == 0) carry = vtx_state(g, xy[vb - 1], w.nrows);
   double2 wc = make_double2(0.0, 0.0);
   if (vb + lane < ve) wc = xy[vb + lane];
   int nq = 0;
@@ -245,7 +247,7 @@ __device__ __forceinline__ void warp_pass(const Geo& geo, const Grid& g, unsigne
       }
       start = start || va == geo.vertex_offsets[ring];
     }
-    const VtxState cur = vtx_state(g, wc);
+    const VtxState cur = vtx_state(g, wc, w.nrows);
     const VtxState prv = rotate_prev(cur, carry, lane);
     bool push = false;
     QEnt e;
@@ -333,16 +335,16 @@ __device__ __forceinline__ void stage_flush(WarpScratch& ws, int& st_n, const Re
 // round; rows are contiguous runs of lanes, so the parity of the set bits
 // before each word comes from a row-segmented XOR scan plus the carry of the
 // previous round.
-__device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw, int r0, int col0, unsigned band,
-                                             unsigned part, const Grid& g, WarpScratch& ws, int& st_n,
+__device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw, int r0, int col0,
+                                             const PartPlan& pl, unsigned part, WarpScratch& ws, int& st_n,
                                              const RecBuf& rb, unsigned* bucket_count, Ctrl* ctrl,
                                              unsigned long long& npix) {
   const int lane = threadIdx.x & 31;
   const int nw = nr * bw;
   const float inv_bw = 1.0f / (float)bw;
-  const unsigned wpr = g.ntx * WPT;  // record words per raster row
-  const unsigned band_wid = band * (unsigned)g.nrows;
-  const unsigned w0 = (unsigned)col0 >> 5;
+  const unsigned wpr = pl.wpr;  // record words per raster row
+  const unsigned w0 = pl.wid0 + ((unsigned)col0 >> 5);
+  const unsigned flags = part | pl.flags;
   int c_row = -1;
   unsigned c_par = 0;
   for (int i0 = 0; i0 < nw; i0 += 32) {
@@ -383,8 +385,8 @@ __device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw,
     if (cnt > STAGE_CAP - st_n) stage_flush(ws, st_n, rb, bucket_count, ctrl);
     if (emit) {
       const int k = st_n + __popc(m & ((1u << lane) - 1u));
-      ws.st_wid[k] = (band_wid + (unsigned)(r0 + row)) * wpr + w0 + (unsigned)wd;
-      ws.st_part[k] = part | g.poly_flags;
+      ws.st_wid[k] = (unsigned)(r0 + row) * wpr + w0 + (unsigned)wd;
+      ws.st_part[k] = flags;
       ws.st_mask[k] = cov;
       npix += (unsigned long long)__popc(cov);
     }
@@ -446,6 +448,8 @@ __device__ __forceinline__ PolyWin make_window(const PartPlan& pl, int k) {
   win.col0 = pl.col0;
   win.bw = pl.bw;
   win.nbits = pl.bw * 32;
+  win.nrows = pl.nrows;
+  win.ncols = pl.ncols;
   return win;
 }
 
@@ -510,7 +514,7 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
       }
       __syncwarp();
     }
-    warp_extract(bm, nr, bw, win.r0, win.col0, pl.band, (unsigned)p, g, ws, st_n, sb, bucket_count, ctrl, npix);
+    warp_extract(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix);
     stage_flush(ws, st_n, sb, bucket_count, ctrl);  // the stage aliases the queue of the next window
     ++wi;
   }
@@ -578,7 +582,7 @@ __global__ void __launch_bounds__(POLY_THREADS) k_poly_spans(Geo geo, Grid g, co
       }
       __syncthreads();
     }
-    warp_extract(bm + rlo * bw, rhi - rlo, bw, win.r0 + rlo, win.col0, pl.band, (unsigned)p, g, ws, st_n, sb,
+    warp_extract(bm + rlo * bw, rhi - rlo, bw, win.r0 + rlo, win.col0, pl, (unsigned)p, ws, st_n, sb,
                  bucket_count, ctrl, npix);
     stage_flush(ws, st_n, sb, bucket_count, ctrl);
     __syncthreads();

@@ -27,14 +27,12 @@ __global__ void k_part_rank(const unsigned* __restrict__ sorted_parts, unsigned 
 
 // key = band-major part rank << 32 | word id within the band's raster
 __global__ void k_rec_keys(RecBuf rb, unsigned long long n, const unsigned* __restrict__ prank,
-                           const PartPlan* __restrict__ plan, unsigned band_words, unsigned long long* keys,
-                           unsigned* vals) {
+                           const PartPlan* __restrict__ plan, unsigned long long* keys, unsigned* vals) {
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n; i += stride) {
     const unsigned part = rb.part[i] & REC_PART_MASK;
-    const unsigned band = plan[part].band;
     const unsigned pr = prank ? prank[part] : part;
-    keys[i] = ((unsigned long long)pr << 32) | (rb.wid[i] - band * band_words);
+    keys[i] = ((unsigned long long)pr << 32) | (rb.wid[i] - plan[part].wid0);
     vals[i] = (unsigned)i;
   }
 }
@@ -61,7 +59,7 @@ template <int VB>
 __global__ void k_sparse_emit(const unsigned long long* __restrict__ skeys, const unsigned* __restrict__ svals,
                               unsigned long long n, RecBuf rb, const unsigned* __restrict__ eff,
                               const unsigned long long* __restrict__ offsets, const PartPlan* __restrict__ plan,
-                              unsigned wpr, const void* __restrict__ values, const unsigned* __restrict__ part_geom,
+                              const void* __restrict__ values, const unsigned* __restrict__ part_geom,
                               unsigned long long scalar_bits, unsigned long long* rows, unsigned long long* cols,
                               void* tvals, unsigned long long* band_counts) {
   using V = typename std::conditional<VB == 1, unsigned char,
@@ -73,6 +71,7 @@ __global__ void k_sparse_emit(const unsigned long long* __restrict__ skeys, cons
     if (!m) continue;
     const unsigned part = rb.part[svals[i]] & REC_PART_MASK;
     const unsigned lwid = (unsigned)skeys[i];
+    const unsigned wpr = plan[part].wpr;
     const unsigned long long y = lwid / wpr;
     const unsigned long long x0 = (unsigned long long)(lwid % wpr) * 32u;
     const V v = values ? static_cast<const V*>(values)[part_geom[part]] : (V)scalar_bits;

@@ -99,3 +99,24 @@ def rasterize_device(dt: DeviceTable, info: RasterInfo, *, fn: str, background, 
     if stats is not None:
         stats.update(st.as_dict())
     return out
+
+
+def rasterize_batch_device(jobs: list, *, dtype: str, outs: list | None = None, all_touched: bool = False,
+                           wave_bytes: int = 0, context: _lib.Context | None = None, stats: dict | None = None):
+    """``rz_rasterize_batch`` on device-resident jobs: each ``BatchJob``
+    holds a DeviceTable and values as a CUDA tensor of the dtype's bits (or a
+    scalar or None); the rasters are written into CUDA tensors (allocated
+    when `outs` is None, one (1, nrows, ncols) raster per job)."""
+    from .engine import run_batch
+
+    torch = _torch()
+    np_dt = np.dtype(dtype)
+    if outs is None:
+        outs = []
+        for j in jobs:
+            n = j.info.nrows * j.info.ncols
+            outs.append(torch.empty(max(1, n * np_dt.itemsize), dtype=torch.uint8,
+                                    device=j.table.tensors["xy"].device))
+    flags = _lib.FLAG_INPUT_DEVICE | _lib.FLAG_OUTPUT_DEVICE | (_lib.FLAG_ALL_TOUCHED if all_touched else 0)
+    run_batch(jobs, outs, [o.data_ptr() for o in outs], dtype, flags, wave_bytes, context, stats, device=True)
+    return outs

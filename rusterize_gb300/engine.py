@@ -6,6 +6,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass
+from typing import Any
 
 import numpy as np
 
@@ -187,3 +188,88 @@ def rasterize_table_sparse(table: GeometryTable, info: RasterInfo, *, values=Non
         stats.update(st_c.as_dict())
     return band_counts, rows, cols, vals
 
+
+
+@dataclass
+class BatchJob:
+    """One job of ``rasterize_batch``: the arguments of one single-band burn.
+
+    values: None (burn 1), a scalar, or a per-geometry array of the batch
+    dtype (host arrays for ``rasterize_batch``; CUDA tensors of the dtype's
+    bits for ``device.rasterize_batch_device``)."""
+
+    table: Any  # GeometryTable, or device.DeviceTable for the device form
+    info: RasterInfo
+    values: Any = None
+    fn: str = "last"
+    background: Any = 0
+
+
+def _job_struct(job: BatchJob, np_dt: np.dtype, keep: list, device: bool) -> _lib.RzJob:
+    """The rz_job of one BatchJob; host buffers it points at go into `keep`."""
+    if job.fn not in _lib.PIXEL_FNS:
+        raise ValueError("Unknown pixel function")
+    j = _lib.RzJob()
+    j.geoms = job.table.c_view()
+    j.info = job.info.c_struct()
+    j.fn = _lib.PIXEL_FNS[job.fn]
+    j.flags = 0
+    bg = np.array([job.background], dtype=np_dt)
+    keep.append(bg)
+    j.background = bg.ctypes.data
+    v = job.values
+    if v is None:
+        j.values = None
+    elif np.isscalar(v) or (isinstance(v, np.ndarray) and v.ndim == 0):
+        sv = np.array([v], dtype=np_dt)
+        keep.append(sv)
+        j.values = sv.ctypes.data
+        j.flags |= _lib.FLAG_SCALAR_VALUE
+    elif device:
+        if v.numel() != job.table.table.n_geoms or v.element_size() != np_dt.itemsize:
+            raise ValueError("Geometry and field lengths must match")
+        j.values = v.data_ptr()
+    else:
+        arr = np.ascontiguousarray(v, dtype=np_dt)
+        if len(arr) != job.table.n_geoms:
+            raise ValueError("Geometry and field lengths must match")
+        keep.append(arr)
+        j.values = arr.ctypes.data
+    return j
+
+
+def run_batch(jobs: list[BatchJob], outs: list, out_ptrs: list[int], dtype: str, flags: int, wave_bytes: int,
+              context: _lib.Context | None, stats: dict | None, device: bool) -> None:
+    """One rz_rasterize_batch call over `jobs` writing `out_ptrs`."""
+    lib = _lib.load()
+    if dtype not in _lib.DTYPES:
+        raise ValueError(f"Unsupported dtype {dtype!r}")
+    np_dt = np.dtype(dtype)
+    ctx = context or _lib.default_context()
+    keep: list = [outs]
+    arr = (_lib.RzJob * max(1, len(jobs)))()
+    for i, job in enumerate(jobs):
+        arr[i] = _job_struct(job, np_dt, keep, device)
+        arr[i].out = out_ptrs[i]
+    st = _lib.RzBatchStats()
+    e = _lib.errbuf()
+    with ctx.lock:
+        rc = lib.rz_rasterize_batch(ctx.handle, arr, len(jobs), _lib.DTYPES[dtype], flags, int(wave_bytes),
+                                    ctypes.byref(st), e, len(e))
+    _lib.raise_for(rc, e.value)
+    if stats is not None:
+        stats.update(st.as_dict())
+
+
+def rasterize_batch(jobs: list[BatchJob], *, dtype: str = "float64", all_touched: bool = False,
+                    wave_bytes: int = 0, context: _lib.Context | None = None,
+                    stats: dict | None = None) -> list[np.ndarray]:
+    """Burn many independent jobs (host geometry tables) in one engine call
+    (``rz_rasterize_batch``): one pass of the kernels per wave of jobs instead
+    of one per job.  Returns one (1, nrows, ncols) array per job, each
+    identical to ``rasterize_table`` of that job alone."""
+    np_dt = np.dtype(dtype)
+    outs = [np.empty((1, j.info.nrows, j.info.ncols), dtype=np_dt) for j in jobs]
+    flags = _lib.FLAG_ALL_TOUCHED if all_touched else 0
+    run_batch(jobs, outs, [o.ctypes.data for o in outs], dtype, flags, wave_bytes, context, stats, device=False)
+    return outs

@@ -175,3 +175,30 @@ def mixed(seed: int = 1003, scale: float = 1.0) -> tuple[Workload, Workload]:
                  {"band_names": names})
     b = Workload(f"mixed_max_int32_{int(side)}", t, cat.astype(np.int32), ext, (1.0, 1.0), "max", "int32", 0.0)
     return a, b
+
+
+BATCH_FNS = ("sum", "min", "max", "first", "last", "count")
+
+
+def batch_jobs(seed: int = 1004, n_jobs: int = 4096, side_range: tuple = (256.0, 8192.0),
+               max_polygons: int = 50_000) -> list[Workload]:
+    """Independent jobs of uneven size: polygons per job lognormal (median
+    500, sigma_ln 1) clipped to [10, max_polygons], 8-256 vertices each; raster
+    side log-uniform over `side_range` at resolution 1; radius lognormal
+    (median 0.02 side, sigma_ln 1) clipped to [2, 0.25 side]; f32 values
+    U[0, 1); pixel function uniform over BATCH_FNS; float32 output, NaN
+    background."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    lo, hi = np.log(side_range[0]), np.log(side_range[1])
+    for j in range(n_jobs):
+        n = int(np.clip(round(float(np.exp(np.log(500.0) + rng.normal(0.0, 1.0)))), 10, max_polygons))
+        side = float(round(float(np.exp(rng.uniform(lo, hi)))))
+        radius = np.clip(np.exp(np.log(0.02 * side) + rng.normal(0.0, 1.0, n)), 2.0, 0.25 * side)
+        cx, cy = rng.uniform(0, side, n), rng.uniform(0, side, n)
+        t = star_polygons(rng, n, (8, 256), radius, cx, cy)
+        values = rng.uniform(0, 1, n).astype(np.float32)
+        fn = BATCH_FNS[int(rng.integers(0, len(BATCH_FNS)))]
+        jobs.append(Workload(f"batch_job_{j}", t, values, (0.0, 0.0, side, side), (1.0, 1.0), fn, "float32",
+                             float("nan")))
+    return jobs
