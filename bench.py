@@ -293,6 +293,9 @@ def run_gb300(args) -> None:
                 "gbs_per_phase": {k: v[2] / (v[1] / 1e3) / 1e9 for k, v in phases.items()},
                 "phase_ms": phase}
 
+    batched = _batched_leg(args, ctx, local) if (world == 1 and args.batch_jobs > 0) else None
+    served = _served_leg(args, local) if (world == 1 and args.serve_seconds > 0) else None
+
     cpu = None
     if rank == 0 and world == 1 and args.cpu_baseline:
         s, cpx, _ = _oracle_step(w, info, threads=1)
@@ -314,10 +317,170 @@ def run_gb300(args) -> None:
             "gpu_launches": launches,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "batched": batched,
+            "served": served,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _batched_leg(args, ctx, local) -> dict:
+    """Uneven independent jobs (synth.batch_jobs: polygons per job lognormal
+    median 500, sides log-uniform 256-8192, f32, pixel functions drawn per
+    job), device-resident: the plain path (one rz_rasterize per job) against
+    the batched form (rz_rasterize_batch over all jobs), jobs/s and px/s."""
+    import torch
+
+    import rusterize_gb300 as rz
+    from rusterize_gb300 import synth
+    from rusterize_gb300.device import DeviceTable, rasterize_batch_device, rasterize_device, upload
+    from rusterize_gb300.engine import BatchJob
+
+    ws = synth.batch_jobs(seed=1004, n_jobs=args.batch_jobs)
+    dev = torch.device("cuda", local)
+    jobs, outs = [], []
+    for w in ws:
+        info = rz.raster_info(w.table, res=w.res, extent=w.extent)
+        jobs.append(BatchJob(DeviceTable.upload(w.table, device=local), info, upload(w.values, device=local), w.fn,
+                             w.background))
+        outs.append(torch.empty(info.nrows * info.ncols * 4, dtype=torch.uint8, device=dev))
+    px = sum(j.info.nrows * j.info.ncols for j in jobs)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+
+    def plain():
+        for j, o in zip(jobs, outs):
+            rasterize_device(j.table, j.info, fn=j.fn, background=j.background, dtype="float32", values=j.values,
+                             out=o, context=ctx)
+
+    st: dict = {}
+
+    def batch():
+        rasterize_batch_device(jobs, dtype="float32", outs=outs, context=ctx, stats=st)
+
+    def timed(f, reps):
+        for _ in range(args.batch_warmup):
+            f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_plain = timed(plain, args.batch_steps)
+    ms_batch = timed(batch, args.batch_steps)
+    n = len(jobs)
+    out = {
+        "workload": f"uneven_jobs_{n}_sides_256-8192_f32",
+        "jobs": n, "polygons": int(sum(j.table.table.n_geoms for j in jobs)), "raster_px": int(px),
+        "plain": {"ms": ms_plain, "jobs_per_s": n / (ms_plain / 1e3), "px_per_s": px / (ms_plain / 1e3)},
+        "batched": {"ms": ms_batch, "jobs_per_s": n / (ms_batch / 1e3), "px_per_s": px / (ms_batch / 1e3),
+                    "waves": st.get("waves"), "kernel_launches": st.get("kernel_launches")},
+        "note": "device-resident geometry and rasters; CUDA events on the engine stream; outputs larger than L2",
+    }
+    del jobs, outs
+    torch.cuda.empty_cache()
+    return out
+
+
+def _served_leg(args, local) -> dict:
+    """A served stream: Poisson arrivals drawn from a pool of uneven jobs
+    (sides log-uniform 256-16384, float32 and uint8 outputs) whose geometry
+    is resident on the device, for `serve_seconds` per rate.  The batching
+    server (two streams, 120 GB admission budget) against the same server
+    with one job per call on one stream (the plain path).  Each result is
+    released as soon as it completes."""
+    import torch
+
+    import rusterize_gb300 as rz
+    from rusterize_gb300 import synth
+    from rusterize_gb300.device import DeviceTable, upload
+    from rusterize_gb300.engine import BatchJob
+    from rusterize_gb300.serve import BurnServer
+
+    ws = synth.batch_jobs(seed=1005, n_jobs=args.serve_pool, side_range=(256.0, 16384.0))
+    pool = []
+    for i, w in enumerate(ws):
+        dtype = "float32" if i % 2 == 0 else "uint8"
+        vals = w.values if dtype == "float32" else (1 + w.values * 254).astype(np.uint8)
+        info = rz.raster_info(w.table, res=w.res, extent=w.extent)
+        bg = w.background if dtype == "float32" else 0
+        pool.append((BatchJob(DeviceTable.upload(w.table, device=local), info, upload(vals, device=local), w.fn, bg),
+                     dtype))
+    free, _ = torch.cuda.mem_get_info(local)
+    budget = int(min(args.serve_budget_gb * (1 << 30), 0.4 * free))
+
+    def run(rate, batched):
+        rng = np.random.default_rng(int(rate) * 7 + batched)
+        lat, errors, lock = [], [], threading.Lock()
+        done = threading.Event()
+        n_sub = [0]
+
+        def on_done(f):
+            r = None
+            try:
+                r = f.result()
+            except BaseException as e:  # a failed request still ends
+                with lock:
+                    errors.append(repr(e)[:200])
+            with lock:
+                if r is not None:
+                    lat.append(r.latency)
+                finished = len(lat) + len(errors) == n_sub[0] and closed[0]
+            if r is not None:
+                r.release()
+            if finished:
+                done.set()
+
+        closed = [False]
+        srv = BurnServer(device=local, budget_bytes=budget, streams=2 if batched else 1,
+                         max_batch=args.serve_max_batch if batched else 1)
+        try:
+            t0 = time.perf_counter()
+            t_next = t0
+            while True:
+                t_next += float(rng.exponential(1.0 / rate))
+                if t_next - t0 > args.serve_seconds:
+                    break
+                delay = t_next - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                job, dtype = pool[int(rng.integers(0, len(pool)))]
+                with lock:
+                    n_sub[0] += 1
+                srv.submit(job, dtype=dtype).add_done_callback(on_done)
+            with lock:
+                closed[0] = True
+                if len(lat) + len(errors) == n_sub[0]:
+                    done.set()
+            done.wait(300)
+            t_end = time.perf_counter()
+            batches = srv.batches
+        finally:
+            srv.close()
+        a = np.array(lat) * 1e3
+        if errors:
+            print(f"served leg: {len(errors)} failed requests, first: {errors[0]}", file=sys.stderr)
+        return {"submitted": n_sub[0], "completed": len(lat), "failed": len(errors),
+                "jobs_per_s": len(lat) / (t_end - t0),
+                "p50_ms": float(np.percentile(a, 50)) if len(a) else None,
+                "p99_ms": float(np.percentile(a, 99)) if len(a) else None, "batches": batches,
+                "drain_s": t_end - t0 - args.serve_seconds}
+
+    rates = []
+    for rate in [float(r) for r in args.serve_rates.split(",") if r]:
+        row = {"rate": rate, "batched": run(rate, True)}
+        if rate <= args.serve_plain_max_rate:
+            row["plain"] = run(rate, False)
+        rates.append(row)
+    del pool
+    torch.cuda.empty_cache()
+    return {"workload": f"served_pool_{len(ws)}_sides_256-16384_f32_u8", "seconds_per_rate": args.serve_seconds,
+            "budget_bytes": budget, "max_batch": args.serve_max_batch, "rates": rates,
+            "note": "Poisson arrivals; latency = completion - submission; throughput over arrival window + drain"}
 
 
 def main():
@@ -330,6 +493,15 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--batch-jobs", type=int, default=512, help="jobs of the batched leg (0: skip it)")
+    ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--batch-warmup", type=int, default=1)
+    ap.add_argument("--serve-seconds", type=float, default=4.0, help="arrival window per rate (0: skip)")
+    ap.add_argument("--serve-rates", default="200,1000,5000")
+    ap.add_argument("--serve-plain-max-rate", type=float, default=1000.0)
+    ap.add_argument("--serve-pool", type=int, default=96)
+    ap.add_argument("--serve-budget-gb", type=float, default=32.0)
+    ap.add_argument("--serve-max-batch", type=int, default=512)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -257,8 +257,9 @@ typedef struct {
  * the engine's kernels per wave instead of one pass per job.  Every job's
  * raster is bit-identical to what rz_rasterize returns for it alone.
  *
- * Jobs are grouped, in order, into waves whose device footprint (rasters,
- * when they are not device outputs, plus geometry tables) stays within
+ * Jobs are grouped, in order, into waves whose estimated device footprint
+ * (rasters when they are not device outputs, geometry and part tables, and
+ * coverage records at about 4 bytes per raster pixel) stays within
  * `wave_bytes` (0: 8 GiB); a job larger than that runs as a wave of its own.
  * `flags`: RZ_FLAG_INPUT_DEVICE, RZ_FLAG_OUTPUT_DEVICE, RZ_FLAG_ALL_TOUCHED
  * (for every job), RZ_FLAG_NO_TIMING.  The call returns after every output

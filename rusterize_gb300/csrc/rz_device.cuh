@@ -69,6 +69,7 @@ enum : unsigned {
   ERR_TOO_WIDE = 5,    // polygon part wider than the bitmap
   ERR_LINE_LONG = 6,   // segment needs more than LINE_MAX_STEPS steps
   ERR_BAD_JOB = 7,     // a batch job's table does not start at 0 / end at its counts
+  ERR_RANGE = 8,       // a record or a raster tile outside the call's buckets (an engine defect)
 };
 
 // Device control block, reset at the start of every pass.
@@ -144,6 +145,7 @@ struct RecBuf {
   unsigned* part;  // part | DEDUP_BIT
   unsigned* mask;  // covered pixels of the word
   unsigned long long cap;
+  unsigned long long nbuckets;  // buckets of the call: every record's bucket is below
 };
 
 __device__ __forceinline__ void set_error(Ctrl* c, unsigned code, unsigned long long idx) {
@@ -214,6 +216,10 @@ __device__ __forceinline__ void emit_run(const RecBuf& rb, unsigned* bucket_coun
     const int lo = max(xs, wd << 5) - (wd << 5), hi = min(xe, (wd << 5) + 32) - (wd << 5);
     const unsigned mask = (hi == 32 ? 0xFFFFFFFFu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
     const unsigned wid = row_wid + (unsigned)wd;
+    if (wid / WPT >= rb.nbuckets) {  // never taken: parts are clipped to their raster
+      set_error(ctrl, ERR_RANGE, wid);
+      return;
+    }
     cg::coalesced_group grp = cg::coalesced_threads();
     unsigned long long slot0 = 0;
     if (grp.thread_rank() == 0) slot0 = atomicAdd(&ctrl->span_count, (unsigned long long)grp.size());

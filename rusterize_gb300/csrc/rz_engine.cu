@@ -38,13 +38,20 @@ cudaError_t ensure(DevBuf& b, size_t need) {
   b.p = nullptr;
   b.cap = 0;
   size_t want = need + need / 8 + (1u << 20);
-  cudaError_t e = cudaMalloc(&b.p, want);
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, want);
   if (e != cudaSuccess) {
     cudaGetLastError();
     want = need;
-    e = cudaMalloc(&b.p, want);
+    p = nullptr;
+    e = cudaMalloc(&p, want);
   }
-  if (e == cudaSuccess) b.cap = want;
+  if (e == cudaSuccess) {
+    b.p = p;
+    b.cap = want;
+  } else {
+    cudaGetLastError();  // an allocation failure is reported here, not by a later call
+  }
   return e;
 }
 
@@ -126,6 +133,9 @@ rz_status ctrl_error(const Ctrl& hc, char* err, size_t errlen) {
                   BITMAP_WORDS * 32 - 64);
     case ERR_LINE_LONG:
       return fail(err, errlen, RZ_VALUE_ERROR, "line segment at vertex %llu spans more than 2^26 pixels", ix);
+    case ERR_RANGE:
+      return fail(err, errlen, RZ_RUNTIME_ERROR, "internal error: record or tile outside the call's rasters (%llu)",
+                  ix);
     case ERR_BAD_JOB:
       return fail(err, errlen, RZ_INVALID_ARGUMENT,
                   "geometry table of job %llu does not start at 0 or end at its own counts", ix);
@@ -545,6 +555,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[7], s));
     RecBuf sb;
     sb.cap = cap;
+    sb.nbuckets = nbuckets;
     sb.wid = static_cast<unsigned*>(ctx->spans.p);
     sb.part = sb.wid + cap;
     sb.mask = sb.part + cap;
@@ -569,7 +580,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     fa.scalar = scalar_bits;
     fa.out = d_out;
     set_background(fa, bg_bits, tsize);
-    fa.nrows = (int)nrows;
+    fa.nrows = (int)(nb * nrows);  // rows of the band stack
     fa.ncols = (int)ncols;
     fa.ntx = ntx;
     fa.big = big;
@@ -599,10 +610,10 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
         want = 0xFFFFFFF0ull;
       }
       cap = want;
-      ctx->span_cap_hint = cap;
       ++reruns;
       continue;
     }
+    ctx->span_cap_hint = std::max(ctx->span_cap_hint, cap);  // only once a pass fitted
     if (stats) {
       stats->edges = hc.edges;
       stats->crossings = hc.crossings;
@@ -617,6 +628,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     const unsigned long long n = ctx->h_ctrl->span_count;
     RecBuf sbr;
     sbr.cap = cap;
+    sbr.nbuckets = nbuckets;
     sbr.wid = static_cast<unsigned*>(ctx->spans.p);
     sbr.part = sbr.wid + cap;
     sbr.mask = sbr.part + cap;
@@ -947,6 +959,7 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
   RecBuf sb;
   sb.cap = cap;
+  sb.nbuckets = nbuckets;
   sb.wid = static_cast<unsigned*>(at(o_spans));
   sb.part = sb.wid + cap;
   sb.mask = sb.part + cap;
@@ -968,7 +981,7 @@ extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const
   fa.scalar = scalar_bits;
   fa.out = out;
   set_background(fa, bg_bits, tsize);
-  fa.nrows = (int)nrows;
+  fa.nrows = (int)(nb * nrows);  // rows of the band stack
   fa.ncols = (int)ncols;
   fa.ntx = ntx;
   fa.big = big;
@@ -1170,7 +1183,9 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
                        base[(size_t)BK_GEOM * (n + 1) + j]);
     fj[j].bucket0 = bucket0[j];
     fj[j].out = out_dev ? jb.out : static_cast<void*>(static_cast<char*>(ctx->out.p) + out_off[j]);
+    fj[j].nrows = (int)b.nrows;
     fj[j].ncols = (int)b.ncols;
+    fj[j].pad = 0;
     fj[j].ntx = (unsigned)b.ntx;
   }
   if (!in_dev) {
@@ -1273,6 +1288,7 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
     cap = std::min<unsigned long long>(cap, (ctx->spans.cap - 16) / RECORD_BYTES) & ~1ull;
     RecBuf sb;
     sb.cap = cap;
+    sb.nbuckets = nbuckets;
     sb.wid = static_cast<unsigned*>(ctx->spans.p);
     sb.part = sb.wid + cap;
     sb.mask = sb.part + cap;
@@ -1334,10 +1350,12 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
         want = 0xFFFFFFF0ull;
       }
       cap = want;
-      ctx->span_cap_hint = cap;
       ++reruns;
       continue;
     }
+    // remembered for the next call only once a pass fitted: a failed
+    // allocation must not make every later call ask for the same size
+    ctx->span_cap_hint = std::max(ctx->span_cap_hint, cap);
     if (stats) {
       stats->edges += hc.edges;
       stats->records += hc.span_count;
@@ -1427,8 +1445,10 @@ extern "C" rz_status rz_rasterize_batch(rz_context* ctx, const rz_job* jobs, siz
       std::memcpy(&b.scalar_bits, jb.values, tsize);
     }
     const size_t geo_bytes = 8 * (b.G + 1) + b.P + 8 * (b.P + 1) + 8 * (b.R + 1) + 16 * b.V + tsize * b.G;
+    // device footprint: rasters (host outputs), geometry, part tables, bucket
+    // tables, and about 4 B of coverage records per raster pixel
     b.dev_bytes = (out_dev ? 0 : b.out_elems * tsize) + geo_bytes * (in_dev ? 1 : 2) +
-                  b.P * (4 + sizeof(PartPlan) + 16 * PC_N + 16) + 16 * b.buckets;
+                  b.P * (4 + sizeof(PartPlan) + 16 * PC_N + 16) + 16 * b.buckets + 4 * b.out_elems;
     total_out += b.out_elems * tsize;
   }
   if (stats) {

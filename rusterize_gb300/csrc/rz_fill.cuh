@@ -19,8 +19,8 @@ namespace rzd {
 struct FillJob {
   unsigned long long bucket0;  // first bucket of the job (in the call's numbering)
   void* out;                   // (nrows, ncols) raster of the job
-  int ncols;
-  unsigned ntx;
+  int nrows, ncols;
+  unsigned ntx, pad;
 };
 
 struct FillArgs {
@@ -46,12 +46,16 @@ struct FillArgs {
   unsigned long long bucket0;
 };
 
+__device__ __forceinline__ unsigned long long gb_of(const FillArgs& a, unsigned long long b) {
+  return a.jobs ? a.bucket0 + b : b;
+}
+
 // The raster tile of bucket b: its first pixel and its width (the last tile
 // of a row is cut at ncols).
 template <typename T>
 __device__ __forceinline__ T* bucket_tile(const FillArgs& a, unsigned long long b, int& len) {
   T* out;
-  int ncols;
+  int nrows, ncols;
   unsigned ntx, lb;
   if (a.jobs) {
     const unsigned long long gb = a.bucket0 + b;
@@ -62,11 +66,13 @@ __device__ __forceinline__ T* bucket_tile(const FillArgs& a, unsigned long long 
     }
     const FillJob j = a.jobs[lo];
     out = static_cast<T*>(j.out);
+    nrows = j.nrows;
     ncols = j.ncols;
     ntx = j.ntx;
     lb = (unsigned)(gb - j.bucket0);
   } else {
     out = static_cast<T*>(a.out);
+    nrows = a.nrows;  // all bands: rows of the (bands * nrows) stack
     ncols = a.ncols;
     ntx = a.ntx;
     lb = (unsigned)b;
@@ -74,6 +80,11 @@ __device__ __forceinline__ T* bucket_tile(const FillArgs& a, unsigned long long 
   const unsigned rowid = lb / ntx;  // 32-bit: a 64-bit divide runs on the FP64 pipe
   const int c0 = (int)(lb - rowid * ntx) << TW_SHIFT;
   len = min(TW, ncols - c0);
+  if (rowid >= (unsigned)nrows) {  // never taken: the buckets of a fill are its rasters' tiles
+    if ((threadIdx.x & 31) == 0) set_error(a.ctrl, ERR_RANGE, gb_of(a, b));
+    len = 0;
+    return out;
+  }
   return out + (unsigned long long)rowid * (unsigned long long)ncols + c0;
 }
 

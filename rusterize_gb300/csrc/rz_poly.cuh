@@ -323,7 +323,10 @@ __device__ __forceinline__ void stage_flush(WarpScratch& ws, int& st_n, const Re
     }
     const unsigned bucket = valid ? wid / WPT : 0xFFFFFFFFu;
     const unsigned same = __match_any_sync(0xFFFFFFFFu, bucket);
-    if (valid && (__ffs(same) - 1) == lane) atomicAdd(&bucket_count[bucket], (unsigned)__popc(same));
+    if (valid && (__ffs(same) - 1) == lane) {
+      if (bucket < rb.nbuckets) atomicAdd(&bucket_count[bucket], (unsigned)__popc(same));
+      else set_error(ctrl, ERR_RANGE, wid);  // never taken: windows are clipped to their raster
+    }
   }
   st_n = 0;
   __syncwarp();
