@@ -260,7 +260,7 @@ typedef struct {
  * Jobs are grouped, in order, into waves whose estimated device footprint
  * (rasters when they are not device outputs, geometry and part tables, and
  * coverage records at about 4 bytes per raster pixel) stays within
- * `wave_bytes` (0: 8 GiB); a job larger than that runs as a wave of its own.
+ * `wave_bytes` (0: 32 GiB); a job larger than that runs as a wave of its own.
  * `flags`: RZ_FLAG_INPUT_DEVICE, RZ_FLAG_OUTPUT_DEVICE, RZ_FLAG_ALL_TOUCHED
  * (for every job), RZ_FLAG_NO_TIMING.  The call returns after every output
  * is written. */

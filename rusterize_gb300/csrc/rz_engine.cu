@@ -1399,7 +1399,7 @@ extern "C" rz_status rz_rasterize_batch(rz_context* ctx, const rz_job* jobs, siz
   const size_t tsize = rz_dtype_size(dt);
   if (tsize == 0) return fail(err, errlen, RZ_VALUE_ERROR, "Unsupported dtype");
   const bool in_dev = flags & RZ_FLAG_INPUT_DEVICE, out_dev = flags & RZ_FLAG_OUTPUT_DEVICE;
-  if (!wave_bytes) wave_bytes = 8ull << 30;
+  if (!wave_bytes) wave_bytes = 32ull << 30;
   // ---- validate every job before any work ----
   std::vector<BatchJob> all(n_jobs);
   unsigned long long total_out = 0;

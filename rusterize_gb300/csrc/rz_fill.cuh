@@ -739,15 +739,17 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
 // one and no intermediate count can equal the background.  `any` is 1
 // wherever the depth is non-zero.  Neither needs values or order.  One warp
 // per bucket (32 consecutive buckets per task, the next bucket's records
-// loaded while the current one is counted); for each word the records of
-// that word are found with a ballot and lane l adds their bit l.
+// loaded while the current one is counted); every record is broadcast to the
+// warp and lane l adds its bit l to the counter of the record's word.
 constexpr int DEPTH_WARPS = 8;
 
 template <typename T, int FN>
 __global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
+  __shared__ unsigned s_cnt[DEPTH_WARPS][WPT * 32];
   Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned* cnt = s_cnt[warp];
   const T bg = from_bits<T>(a.bg);
   const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
   while (true) {
@@ -778,29 +780,29 @@ __global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
         store_bg<T>(dst, len, a.bg16, bg, lane, 32);
         continue;
       }
-      unsigned d[WPT];
+      // lane l owns column l of the tile's 16 words: cnt[w * 32 + l], so the
+      // counters need no atomics and sit in distinct banks
 #pragma unroll
-      for (int w = 0; w < WPT; ++w) d[w] = 0u;
+      for (int w = 0; w < WPT; ++w) cnt[w * 32 + lane] = 0u;
+      __syncwarp();
       for (int i0 = 0; i0 < n; i0 += 32) {
         if (i0 > 0) r = i0 + lane < n ? a.recs[o0 + i0 + lane] : make_uint2(0u, 0u);
-        const unsigned w_of = i0 + lane < n ? (r.x >> REC_W_SHIFT) & 15u : 16u;
-#pragma unroll
-        for (int w = 0; w < WPT; ++w) {
-          unsigned g = __ballot_sync(0xFFFFFFFFu, w_of == (unsigned)w);
-          while (g) {
-            const int src = __ffs(g) - 1;
-            g &= g - 1;
-            d[w] += (__shfl_sync(0xFFFFFFFFu, r.y, src) >> lane) & 1u;
-          }
+        const int m = min(32, n - i0);
+        for (int i = 0; i < m; ++i) {
+          const unsigned x = __shfl_sync(0xFFFFFFFFu, r.x, i);
+          const unsigned y = __shfl_sync(0xFFFFFFFFu, r.y, i);
+          if ((y >> lane) & 1u) ++cnt[((x >> REC_W_SHIFT) & 15u) * 32 + lane];
         }
       }
+      __syncwarp();
 #pragma unroll
       for (int w = 0; w < WPT; ++w) {
+        const unsigned d = cnt[w * 32 + lane];
         T v = bg;
-        if (d[w]) {
+        if (d) {
           if constexpr (FN == F_ANY) v = T(1);
-          else if constexpr (std::is_integral<T>::value) v = (T)(typename std::make_unsigned<T>::type)d[w];
-          else v = (T)d[w];
+          else if constexpr (std::is_integral<T>::value) v = (T)(typename std::make_unsigned<T>::type)d;
+          else v = (T)d;
         }
         if (w * 32 + lane < len) dst[w * 32 + lane] = v;
       }
