@@ -286,8 +286,18 @@ def run_gb300(args) -> None:
     dom_key = max(phases, key=lambda k: phases[k][1])
     dom, dom_ms, dom_bytes = phases[dom_key]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    # DRAM bytes per step of the dominant phase from the ncu capture of this
+    # workload (profiles/dram_traffic.json), when the workload matches
+    traffic, traffic_src = None, None
+    tpath = ROOT / "profiles" / "dram_traffic.json"
+    if tpath.exists():
+        t = json.loads(tpath.read_text())
+        if t.get("workload") == WORKLOAD and float(t.get("scale", -1)) == float(args.scale):
+            traffic = t["phases"].get(dom_key, {}).get("bytes")
+            traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum per step, profiles/dram_traffic.json"
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None,
+                "frac": achieved / hbm, "traffic": traffic, "traffic_source": traffic_src,
+                "traffic_over_algorithmic": (traffic / dom_bytes) if traffic else None,
                 "peak_source": "measured" if not peaks.get("fallback") else "fallback",
                 "algorithmic_bytes_per_step": {"spans": span_bytes, "fill": fill_bytes},
                 "gbs_per_phase": {k: v[2] / (v[1] / 1e3) / 1e9 for k, v in phases.items()},
