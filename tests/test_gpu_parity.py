@@ -217,7 +217,7 @@ def test_degenerate_and_nonfinite():
 
 def test_span_buffer_growth_rerun():
     # steep lines give one span per pixel: > 1M spans from a few hundred
-    # vertices overflow the first span buffer and force the rerun path
+    # vertices overflow the first record buffer and force the rerun path
     rng = np.random.default_rng(4)
     b = G.TableBuilder()
     for _ in range(400):
