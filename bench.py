@@ -42,10 +42,9 @@ METRIC = "burned px/s (large polygon fill: sum f64 + count u32)"
 
 
 def _dist():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", str(rank)))
-    return rank, world, local
+    from rusterize_gb300.shard import dist_env
+
+    return dist_env()
 
 
 def _workload(seed: int, scale: float):
@@ -203,9 +202,7 @@ def run_gb300(args) -> None:
             stats_acc.append((st1, st2))
         return st1, st2
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+    from rusterize_gb300.shard import barrier, max_over_ranks, sum_over_ranks
 
     for _ in range(args.warmup):
         step()
@@ -234,11 +231,13 @@ def run_gb300(args) -> None:
     recs_sum, recs_cnt = acc[0][0]["spans"], acc[0][1]["spans"]
     fill_bytes = acc[0][0]["out_bytes"] + acc[0][1]["out_bytes"] + 8 * (recs_sum + recs_cnt) + 8 * recs_sum
     span_bytes = 2 * 16 * w.table.n_vertices + 12 * (recs_sum + recs_cnt)
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * px_step / (ms / 1e3)
+    # the slowest rank's step time; the pixel writes of every rank (each burns
+    # its own job: seed + rank)
+    dev = torch.device("cuda", local)
+    ms = max_over_ranks(ms, device=dev)
+    px_all = sum_over_ranks(px_step, device=dev)
+    edges_all = sum_over_ranks(edges_step, device=dev)
+    value = px_all / (ms / 1e3)
 
     # e2e: public host API from pinned buffers (H2D + D2H inside the region)
     e2e = None
@@ -272,10 +271,10 @@ def run_gb300(args) -> None:
             host_step()
         e1.record(stream)
         torch.cuda.synchronize()
-        e_ms = e0.elapsed_time(e1) / args.e2e_steps
+        e_ms = max_over_ranks(e0.elapsed_time(e1) / args.e2e_steps, device=dev)
         h2d = sum(a.nbytes for a in (tb.part_offsets, tb.part_kind, tb.ring_offsets, tb.vertex_offsets, tb.xy))
         h2d = 2 * h2d + w.values.nbytes
-        e2e = {"value": world * px_step / (e_ms / 1e3), "unit": "px/s", "ms_per_step": e_ms,
+        e2e = {"value": px_all / (e_ms / 1e3), "unit": "px/s", "ms_per_step": e_ms,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(o_sum.nbytes + o_cnt.nbytes)}
 
     peaks = _measured_peaks()
@@ -320,7 +319,7 @@ def run_gb300(args) -> None:
             "config": {"workload": WORKLOAD, "scale": args.scale, "polygons": w.table.n_geoms,
                        "vertices": w.table.n_vertices, "raster": [info.nrows, info.ncols],
                        "l2": "inputs larger than L2 (vertex table and rasters exceed 129 MB); no flush"},
-            "edges_per_s": world * edges_step / (ms / 1e3),
+            "edges_per_s": edges_all / (ms / 1e3),
             "pixel_writes_per_step": px_step,
             "clocks": clk.summary(),
             "e2e": e2e,
