@@ -7,7 +7,6 @@ import zlib
 import numpy as np
 import pytest
 
-import oracle
 import rusterize_gb300 as rz
 from rusterize_gb300 import geometry as G
 from rusterize_gb300 import synth
