@@ -378,8 +378,9 @@ def _batched_leg(args, ctx, local) -> dict:
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    ms_plain = timed(plain, args.batch_steps)
-    ms_batch = timed(batch, args.batch_steps)
+    legs = set(args.batch_legs.split(","))
+    ms_plain = timed(plain, args.batch_steps) if "plain" in legs else float("nan")
+    ms_batch = timed(batch, args.batch_steps) if "batched" in legs else float("nan")
     n = len(jobs)
     out = {
         "workload": f"uneven_jobs_{n}_sides_256-8192_f32",
@@ -504,6 +505,7 @@ def main():
     ap.add_argument("--batch-jobs", type=int, default=512, help="jobs of the batched leg (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--batch-warmup", type=int, default=1)
+    ap.add_argument("--batch-legs", default="plain,batched", help="legs of the batched comparison to run")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="arrival window per rate (0: skip)")
     ap.add_argument("--serve-rates", default="200,1000,5000")
     ap.add_argument("--serve-plain-max-rate", type=float, default=1000.0)

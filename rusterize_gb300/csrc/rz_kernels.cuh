@@ -113,8 +113,7 @@ __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restr
       long long ylo = 0x7FFFFFFFFFFFFFFFll, yhi = (long long)0x8000000000000000ull;
       long long xlo = 0x7FFFFFFFFFFFFFFFll, xhi = (long long)0x8000000000000000ull;
       int nan_x = 0;
-      for (unsigned long long v = vs + lane; v < ve; v += 32) {
-        const double2 w = geo.xy[v];
+      auto fold = [&](double2 w) {
         const unsigned long long by = f64_bits(w.y), bx = f64_bits(w.x);
         if (!nan_bits(by)) {
           const long long k = (long long)(by ^ ((unsigned long long)((long long)by >> 63) >> 1));
@@ -128,6 +127,14 @@ __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restr
         } else {
           nan_x = 1;
         }
+      };
+      // two loads in flight per lane; min / max are idempotent, so a missing
+      // second vertex folds the first one again
+      for (unsigned long long v = vs + lane; v < ve; v += 64) {
+        const double2 w = geo.xy[v];
+        const double2 w2 = v + 32 < ve ? geo.xy[v + 32] : w;
+        fold(w);
+        fold(w2);
       }
       for (int o = 16; o > 0; o >>= 1) {
         ylo = min(ylo, (long long)__shfl_xor_sync(0xFFFFFFFFu, (unsigned long long)ylo, o));
