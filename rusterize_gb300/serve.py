@@ -200,12 +200,14 @@ class BurnServer:
             if not batch:
                 return
             t0 = time.perf_counter()
+            outs = None
             try:
                 outs = [torch.empty(max(1, r.nbytes), dtype=torch.uint8, device=dev) for r in batch]
                 torch.cuda.current_stream(dev).synchronize()  # allocations ordered before the engine stream
                 rasterize_batch_device([r.job for r in batch], dtype=batch[0].dtype, outs=outs, context=ctx,
                                        wave_bytes=self.wave_bytes)
-            except BaseException as e:  # every request of the batch sees the error
+            except Exception as e:  # every request of the batch sees the error; later batches go on
+                outs = None
                 for r in batch:
                     self._release(r.nbytes)
                     r.future.set_exception(e)
