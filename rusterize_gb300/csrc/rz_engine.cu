@@ -386,6 +386,16 @@ __global__ void k_reset_pass(Ctrl* c) {
   c->fill_work = 0;
 }
 
+// After a failed call: wait for any kernels or copies the call had already
+// queued, so that the caller may free its buffers once the call returns.
+static rz_status drain_on_error(cudaStream_t s, rz_status st) {
+  if (st != RZ_OK && s) {
+    cudaStreamSynchronize(s);
+    cudaGetLastError();  // a failed call reports its own error; nothing is left pending
+  }
+  return st;
+}
+
 // The burn pipeline shared by the dense and the sparse entry points; with
 // `sp` the coverage records are turned into COO triplets instead of being
 // scattered into buckets and filled.
@@ -757,8 +767,9 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
                                   const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
                                   rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats,
                                   char* err, size_t errlen) {
-  return burn_impl(ctx, g, values, background, band_of_geom, n_bands, info, fn, dt, flags, out, stats, err, errlen,
-                   nullptr);
+  return drain_on_error(ctx ? ctx->stream : nullptr,
+                        burn_impl(ctx, g, values, background, band_of_geom, n_bands, info, fn, dt, flags, out, stats,
+                                  err, errlen, nullptr));
 }
 
 extern "C" rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, const void* values,
@@ -771,8 +782,9 @@ extern "C" rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, con
   if (flags & RZ_FLAG_OUTPUT_DEVICE)
     return fail(err, errlen, RZ_INVALID_ARGUMENT, "the sparse encoding returns host arrays");
   auto* sp = new rz_sparse();
-  const rz_status st = burn_impl(ctx, g, values, nullptr, band_of_geom, n_bands, info, fn, dt, flags, nullptr, stats,
-                                 err, errlen, sp);
+  const rz_status st = drain_on_error(ctx ? ctx->stream : nullptr,
+                                      burn_impl(ctx, g, values, nullptr, band_of_geom, n_bands, info, fn, dt, flags,
+                                                nullptr, stats, err, errlen, sp));
   if (st != RZ_OK) {
     delete sp;
     return st;
@@ -824,10 +836,24 @@ NoAllocDevice g_noalloc[kNoAllocMaxDevices];
 
 }  // namespace
 
+static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* values, const void* background,
+                              const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
+                              rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats, char* err,
+                              size_t errlen);
+
 extern "C" rz_status rz_rasterize_noalloc(void* stream, const rz_geoms* g, const void* values,
                                           const void* background, const uint32_t* band_of_geom, uint32_t n_bands,
                                           const rz_raster_info* info, rz_pixel_fn fn, rz_dtype dt, uint32_t flags,
                                           void* out, rz_stats* stats, char* err, size_t errlen) {
+  return drain_on_error(static_cast<cudaStream_t>(stream),
+                        noalloc_impl(stream, g, values, background, band_of_geom, n_bands, info, fn, dt, flags, out,
+                                     stats, err, errlen));
+}
+
+static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* values, const void* background,
+                              const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
+                              rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats, char* err,
+                              size_t errlen) {
   rz::clear_err(err, errlen);
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (!g || !info || !background || !out) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null argument");
@@ -1463,7 +1489,7 @@ extern "C" rz_status rz_rasterize_batch(rz_context* ctx, const rz_job* jobs, siz
   unsigned long long G = 0, P = 0, buckets = 0;
   auto flush = [&]() -> rz_status {
     if (wave.empty()) return RZ_OK;
-    const rz_status st = run_wave(ctx, jobs, wave, dt, flags, stats, err, errlen);
+    const rz_status st = drain_on_error(ctx->stream, run_wave(ctx, jobs, wave, dt, flags, stats, err, errlen));
     wave.clear();
     bytes = 0;
     G = P = buckets = 0;
