@@ -114,7 +114,7 @@ PROTOTYPES = {
     "rz_dtype_size": (c_size_t, [c_int]),
     "rz_pixel_fn_from_str": (c_int, [c_char_p, POINTER(c_int), c_char_p, c_size_t]),
     "rz_parse_wkt": (c_int, [POINTER(c_char_p), POINTER(c_size_t), c_size_t, POINTER(c_void_p), c_char_p, c_size_t]),
-    "rz_parse_wkb": (c_int, [POINTER(c_void_p), POINTER(c_size_t), c_size_t, POINTER(c_void_p), c_char_p, c_size_t]),
+    "rz_parse_wkb": (c_int, [POINTER(c_char_p), POINTER(c_size_t), c_size_t, POINTER(c_void_p), c_char_p, c_size_t]),
     "rz_geom_buffer_view": (c_int, [c_void_p, POINTER(RzGeoms)]),
     "rz_geom_buffer_free": (None, [c_void_p]),
     "rz_raster_info_build": (c_int, [POINTER(RzGeoms), c_uint32, POINTER(c_uint64), POINTER(c_double),

@@ -1,9 +1,14 @@
 // rz_host.cpp -- host side of the boundary: geometry readers (WKT/WKB ->
 // parts table), the raster-grid builder and small enum helpers.  No CUDA here.
+#include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
+#include <cstring>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "rz_internal.h"
 
@@ -82,10 +87,20 @@ struct WktReader {
     size_t j = i;
     while (j < n && (std::isalnum((unsigned char)s[j]) || s[j] == '.' || s[j] == '-' || s[j] == '+')) ++j;
     if (j == i) return false;
-    std::string tok(s + i, j - i);
+    const size_t len = j - i;
+    char stack[64];
+    std::string heap;
+    char* tok = stack;
+    if (len < sizeof(stack)) {
+      std::memcpy(stack, s + i, len);
+      stack[len] = '\0';
+    } else {
+      heap.assign(s + i, len);
+      tok = &heap[0];
+    }
     char* end = nullptr;
-    v = std::strtod(tok.c_str(), &end);
-    if (end != tok.c_str() + tok.size()) return false;
+    v = std::strtod(tok, &end);
+    if (end != tok + len) return false;
     i = j;
     return true;
   }
@@ -260,29 +275,123 @@ void rollback(GeomTable& t, const Mark& m) {
 
 }  // namespace
 
+// ------------------------------------------------------- chunked parse ----
+// Items are parsed in contiguous chunks on several host threads, each chunk
+// into its own table; the tables are then appended in chunk order with their
+// offsets rebased.  The result and the reported error (the first failing
+// item in input order) are those of a sequential parse.
+namespace {
+
+struct ChunkResult {
+  GeomTable t;
+  size_t fail_item = SIZE_MAX;
+  std::string msg;
+};
+
+// parse_one(k, table, msg) -> 1: parsed and kept, 0: parsed and dropped, -1: error
+template <typename ParseOne>
+void parse_chunk(size_t k0, size_t k1, ChunkResult& c, ParseOne&& parse_one) {
+  for (size_t k = k0; k < k1; ++k) {
+    const int r = parse_one(k, c.t, c.msg);
+    if (r < 0) {
+      c.fail_item = k;
+      return;
+    }
+    if (r > 0) c.t.part_offsets.push_back(c.t.part_kind.size());
+  }
+}
+
+void append_table(GeomTable& dst, const GeomTable& src) {
+  const uint64_t p0 = dst.part_kind.size(), r0 = dst.ring_flags.size(), v0 = dst.xy.size() / 2;
+  for (size_t i = 1; i < src.part_offsets.size(); ++i) dst.part_offsets.push_back(src.part_offsets[i] + p0);
+  dst.part_kind.insert(dst.part_kind.end(), src.part_kind.begin(), src.part_kind.end());
+  for (size_t i = 1; i < src.ring_offsets.size(); ++i) dst.ring_offsets.push_back(src.ring_offsets[i] + r0);
+  dst.ring_flags.insert(dst.ring_flags.end(), src.ring_flags.begin(), src.ring_flags.end());
+  for (size_t i = 1; i < src.vertex_offsets.size(); ++i) dst.vertex_offsets.push_back(src.vertex_offsets[i] + v0);
+  dst.xy.insert(dst.xy.end(), src.xy.begin(), src.xy.end());
+}
+
+// threads for n items of `bytes` total input: one per 4 MiB of input, at
+// most the host's hardware threads and 32, and never more than one per 256 items
+unsigned parse_threads(size_t n, size_t bytes) {
+  const char* env = std::getenv("RZ_PARSE_THREADS");
+  if (env && *env) {
+    const long v = std::strtol(env, nullptr, 10);
+    if (v >= 1) return (unsigned)std::min<long>(v, 256);
+  }
+  unsigned hw = std::thread::hardware_concurrency();
+  if (hw == 0) hw = 1;
+  size_t t = std::min<size_t>({(size_t)hw, (size_t)32, bytes / (4u << 20) + 1, n / 256 + 1});
+  return (unsigned)std::max<size_t>(t, 1);
+}
+
+template <typename ParseOne>
+rz_status parse_all(size_t n, size_t bytes, rz_geom_buffer** out, ParseOne&& parse_one, const char* what,
+                    char* err, size_t errlen) {
+  const unsigned T = parse_threads(n, bytes);
+  std::vector<ChunkResult> chunks(T);
+  if (T == 1) {
+    parse_chunk(0, n, chunks[0], parse_one);
+  } else {
+    std::vector<std::thread> ts;
+    ts.reserve(T);
+    for (unsigned c = 0; c < T; ++c) {
+      const size_t k0 = n * c / T, k1 = n * (c + 1) / T;
+      ts.emplace_back([&, c, k0, k1] { parse_chunk(k0, k1, chunks[c], parse_one); });
+    }
+    for (auto& th : ts) th.join();
+  }
+  for (const ChunkResult& c : chunks)  // chunks are in item order: the first failure is the first reported
+    if (c.fail_item != SIZE_MAX)
+      return fail(err, errlen, RZ_PARSE_ERROR, "Cannot parse geometry. Check that the %s valid. (item %zu%s%s)",
+                  what, c.fail_item, c.msg.empty() ? "" : ": ", c.msg.c_str());
+  auto* buf = new rz_geom_buffer();
+  if (T == 1) {
+    buf->t = std::move(chunks[0].t);
+  } else {
+    GeomTable& t = buf->t;
+    size_t G = 0, P = 0, R = 0, V = 0;
+    for (const ChunkResult& c : chunks) {
+      G += c.t.part_offsets.size() - 1;
+      P += c.t.part_kind.size();
+      R += c.t.ring_flags.size();
+      V += c.t.xy.size() / 2;
+    }
+    t.part_offsets.reserve(G + 1);
+    t.part_kind.reserve(P);
+    t.ring_offsets.reserve(P + 1);
+    t.ring_flags.reserve(R);
+    t.vertex_offsets.reserve(R + 1);
+    t.xy.reserve(2 * V);
+    for (const ChunkResult& c : chunks) append_table(t, c.t);
+  }
+  if (buf->t.part_offsets.size() == 1) {
+    delete buf;
+    return fail(err, errlen, RZ_VALUE_ERROR, "Could not parse geometry. Only WKT or WKB formats are supported.");
+  }
+  *out = buf;
+  return RZ_OK;
+}
+
+}  // namespace
+
 extern "C" rz_status rz_parse_wkt(const char* const* texts, const size_t* lens, size_t n,
                                   rz_geom_buffer** out, char* err, size_t errlen) {
   rz::clear_err(err, errlen);
   *out = nullptr;
-  auto* buf = new rz_geom_buffer();
-  GeomTable& t = buf->t;
-  for (size_t k = 0; k < n; ++k) {
-    WktReader r{texts[k], lens[k]};
-    if (!wkt_geometry(r, t, 0) || (r.ws(), r.i != r.n)) {
-      delete buf;
-      return fail(err, errlen, RZ_PARSE_ERROR,
-                  "Cannot parse geometry. Check that the WKT is valid. (item %zu%s%s)", k,
-                  r.msg.empty() ? "" : ": ", r.msg.c_str());
-    }
-    t.part_offsets.push_back(t.part_kind.size());
-  }
-  if (t.part_offsets.size() == 1) {
-    delete buf;
-    return fail(err, errlen, RZ_VALUE_ERROR,
-                "Could not parse geometry. Only WKT or WKB formats are supported.");
-  }
-  *out = buf;
-  return RZ_OK;
+  size_t bytes = 0;
+  for (size_t k = 0; k < n; ++k) bytes += lens[k];
+  return parse_all(
+      n, bytes, out,
+      [&](size_t k, GeomTable& t, std::string& msg) -> int {
+        WktReader r{texts[k], lens[k]};
+        if (!wkt_geometry(r, t, 0) || (r.ws(), r.i != r.n)) {
+          msg = r.msg;
+          return -1;
+        }
+        return 1;
+      },
+      "WKT is", err, errlen);
 }
 
 // ------------------------------------------------------------------ WKB ----
@@ -418,30 +527,24 @@ extern "C" rz_status rz_parse_wkb(const uint8_t* const* blobs, const size_t* len
                                   rz_geom_buffer** out, char* err, size_t errlen) {
   rz::clear_err(err, errlen);
   *out = nullptr;
-  auto* buf = new rz_geom_buffer();
-  GeomTable& t = buf->t;
-  for (size_t k = 0; k < n; ++k) {
-    WkbReader r{blobs[k], lens[k]};
-    Mark m = mark_of(t);
-    if (!wkb_geometry(r, t, 0, 0)) {
-      delete buf;
-      return fail(err, errlen, RZ_PARSE_ERROR,
-                  "Cannot parse geometry. Check that the WKB bytes are valid. (item %zu%s%s)", k,
-                  r.msg.empty() ? "" : ": ", r.msg.c_str());
-    }
-    if (r.drop) {  // try_to_geometry() -> None: silently skipped (parse_geometry.rs:113-115)
-      rollback(t, m);
-      continue;
-    }
-    t.part_offsets.push_back(t.part_kind.size());
-  }
-  if (t.part_offsets.size() == 1) {
-    delete buf;
-    return fail(err, errlen, RZ_VALUE_ERROR,
-                "Could not parse geometry. Only WKT or WKB formats are supported.");
-  }
-  *out = buf;
-  return RZ_OK;
+  size_t bytes = 0;
+  for (size_t k = 0; k < n; ++k) bytes += lens[k];
+  return parse_all(
+      n, bytes, out,
+      [&](size_t k, GeomTable& t, std::string& msg) -> int {
+        WkbReader r{blobs[k], lens[k]};
+        Mark m = mark_of(t);
+        if (!wkb_geometry(r, t, 0, 0)) {
+          msg = r.msg;
+          return -1;
+        }
+        if (r.drop) {  // try_to_geometry() -> None: silently skipped (parse_geometry.rs:113-115)
+          rollback(t, m);
+          return 0;
+        }
+        return 1;
+      },
+      "WKB bytes are", err, errlen);
 }
 
 extern "C" rz_status rz_geom_buffer_view(const rz_geom_buffer* buf, rz_geoms* out) {

@@ -212,10 +212,10 @@ def from_wkt(texts: Sequence[str]) -> GeometryTable:
 def from_wkb(blobs: Sequence[bytes]) -> GeometryTable:
     """Parse WKB blobs (python/src/geo/parse_geometry.rs:77-84,109-120)."""
     lib = _lib.load()
-    enc = [bytes(b) for b in blobs]
+    # bytes objects are passed by pointer (no copy); their lengths bound the reads
+    enc = [b if isinstance(b, bytes) else bytes(b) for b in blobs]
     n = len(enc)
-    keep = [ctypes.create_string_buffer(b, len(b)) for b in enc]
-    ptrs = (ctypes.c_void_p * n)(*[ctypes.addressof(k) for k in keep])
+    ptrs = (ctypes.c_char_p * n)(*enc)
     lens = (ctypes.c_size_t * n)(*[len(x) for x in enc])
     buf = ctypes.c_void_p()
     e = _lib.errbuf()
