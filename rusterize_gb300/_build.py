@@ -23,7 +23,8 @@ OUT_DIR = PKG / "_lib"
 OBJ_DIR = OUT_DIR / "obj"
 LIB_NAME = "librusterize_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-pthread",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 
 
@@ -93,7 +94,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     objs = [OBJ_DIR / (s.name + ".o") for s in srcs]
     lib = lib_path()
     if force or jobs or _stale(lib, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart", "-Xlinker", "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError("link failed:\n" + res.stdout + res.stderr)
