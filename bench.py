@@ -37,6 +37,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOAD = "large_fill_100k_polygons_20000x20000_sum_f64+count_u32"
+REF_BUDGET_S = 90.0  # CPU seconds of warm-up + timed steps in the reference arm
 METRIC = "burned px/s (large polygon fill: sum f64 + count u32)"
 
 
@@ -141,12 +142,25 @@ def _oracle_step(w_sum, info, threads: int = 2) -> tuple[float, int, int]:
 
 
 def run_reference(args) -> None:
+    """The reference arm: the CPU restatement of the reference's burn path
+    (oracle/) on this host, the two burns of a step in two host threads.
+    Each step is a bounded sample of the workload: the same generator at a
+    scale chosen so that warm-up and timed steps together take about
+    REF_BUDGET_S seconds, whatever --steps is."""
     rank, world, _ = _dist()
     if rank != 0:
         return
     import rusterize_gb300 as rz
 
-    w = _workload(1002, args.scale)
+    # probe one step at 1/16 of the area to size the sample
+    probe = _workload(1002, args.scale / 16.0)
+    pinfo = rz.raster_info(probe.table, res=probe.res, extent=probe.extent)
+    t_probe, _, _ = _oracle_step(probe, pinfo)
+    per_step_full = 16.0 * t_probe
+    steps_total = max(1, args.steps + args.warmup)
+    sample = min(1.0, REF_BUDGET_S / (steps_total * per_step_full))
+    scale = args.scale * sample
+    w = probe if abs(scale - args.scale / 16.0) < 1e-12 else _workload(1002, scale)
     info = rz.raster_info(w.table, res=w.res, extent=w.extent)
     for _ in range(args.warmup):
         _oracle_step(w, info)
@@ -156,14 +170,17 @@ def run_reference(args) -> None:
         times.append(s)
     ms = 1e3 * sum(times) / len(times)
     value = px / (ms / 1e3)
+    what = ("the full workload" if sample >= 1.0 else
+            f"the same generator at {sample:.3g} of the workload's area and polygon count "
+            f"({w.table.n_geoms} polygons, {info.nrows} x {info.ncols})")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "px/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "scale": args.scale},
+        "config": {"workload": WORKLOAD, "scale": args.scale, "sample_scale": scale},
         "edges_per_s": edges / (ms / 1e3),
         "cpu_baseline": {"value": value, "unit": "px/s", "cores": 2, "kind": "port",
-                         "sample": "full workload per step: the two burns (sum, count) run in 2 host threads, "
+                         "sample": f"per step {what}: the two burns (sum, count) run in 2 host threads, "
                                    "each single-threaded like the reference's single-band process loop"},
         "e2e": {"value": value, "unit": "px/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
