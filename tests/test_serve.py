@@ -118,3 +118,48 @@ def test_server_backpressure_and_failed_batches():
         ok = srv.submit(jobs[1]).result(timeout=120)
         ok.release()
         assert srv.admission.reserved == 0
+
+
+def test_admission_invariants_under_random_traffic():
+    """Random puts, takes and releases: reservations never exceed the budget,
+    every request leaves exactly once, and requests of one dtype leave in
+    arrival order."""
+    hypothesis = pytest.importorskip("hypothesis")
+    st = hypothesis.strategies
+
+    ops = st.lists(st.one_of(
+        st.tuples(st.just("put"), st.integers(1, 60), st.sampled_from(["float32", "uint8"])),
+        st.tuples(st.just("take"), st.just(0), st.just("")),
+        st.tuples(st.just("release"), st.just(0), st.just("")),
+    ), max_size=80)
+
+    @hypothesis.settings(max_examples=300, deadline=None)
+    @hypothesis.given(ops, st.integers(60, 200), st.integers(1, 8))
+    def run(seq, budget, max_batch):
+        a = Admission(budget_bytes=budget, max_batch=max_batch)
+        held, order, out = [], {}, []
+        for op, nbytes, dtype in seq:
+            if op == "put":
+                r = _req(nbytes, dtype)
+                order.setdefault(dtype, []).append(r)
+                a.put(r)
+            elif op == "take":
+                b = a.take(timeout=0)
+                assert len(b) <= max_batch and len({r.dtype for r in b}) <= 1
+                held.extend(b)
+                out.extend(b)
+            elif held:
+                a.release(held.pop(0).nbytes)
+            assert a.reserved == sum(r.nbytes for r in held) <= budget
+        while held:  # drain: release everything, take the rest
+            a.release(held.pop().nbytes)
+        while len(a):
+            b = a.take(timeout=0)
+            out.extend(b)
+            for r in b:
+                a.release(r.nbytes)
+        assert sorted(map(id, out)) == sorted(id(r) for rs in order.values() for r in rs)
+        for dtype, rs in order.items():
+            assert [r for r in out if r.dtype == dtype] == rs
+
+    run()
