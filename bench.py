@@ -37,7 +37,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOAD = "large_fill_100k_polygons_20000x20000_sum_f64+count_u32"
-REF_BUDGET_S = 90.0  # CPU seconds of warm-up + timed steps in the reference arm
+REF_THREADS = 2  # host threads of both CPU legs: one per burn of a step
 METRIC = "burned px/s (large polygon fill: sum f64 + count u32)"
 
 
@@ -143,48 +143,82 @@ def _oracle_step(w_sum, info, threads: int = 2) -> tuple[float, int, int]:
 
 def run_reference(args) -> None:
     """The reference arm: the CPU restatement of the reference's burn path
-    (oracle/) on this host, the two burns of a step in two host threads.
-    Each step is a bounded sample of the workload: the same generator at a
-    scale chosen so that warm-up and timed steps together take about
-    REF_BUDGET_S seconds, whatever --steps is."""
+    (oracle/) on this host, on the full workload of the GPU arm.  The two
+    burns of a step (sum f64, count u32) run in REF_THREADS host threads, each
+    single-threaded like the reference's single-band `process` loop
+    (rust/src/rasterize.rs:105-113); the GPU arm's cpu_baseline uses the same
+    threads."""
     rank, world, _ = _dist()
     if rank != 0:
         return
     import rusterize_gb300 as rz
 
-    # probe one step at 1/16 of the area to size the sample
-    probe = _workload(1002, args.scale / 16.0)
-    pinfo = rz.raster_info(probe.table, res=probe.res, extent=probe.extent)
-    t_probe, _, _ = _oracle_step(probe, pinfo)
-    per_step_full = 16.0 * t_probe
-    steps_total = max(1, args.steps + args.warmup)
-    sample = min(1.0, REF_BUDGET_S / (steps_total * per_step_full))
-    scale = args.scale * sample
-    w = probe if abs(scale - args.scale / 16.0) < 1e-12 else _workload(1002, scale)
+    w = _workload(1002, args.scale)
     info = rz.raster_info(w.table, res=w.res, extent=w.extent)
     for _ in range(args.warmup):
-        _oracle_step(w, info)
+        _oracle_step(w, info, threads=REF_THREADS)
     times, px, edges = [], 0, 0
     for _ in range(args.steps):
-        s, px, edges = _oracle_step(w, info)
+        s, px, edges = _oracle_step(w, info, threads=REF_THREADS)
         times.append(s)
     ms = 1e3 * sum(times) / len(times)
     value = px / (ms / 1e3)
-    what = ("the full workload" if sample >= 1.0 else
-            f"the same generator at {sample:.3g} of the workload's area and polygon count "
-            f"({w.table.n_geoms} polygons, {info.nrows} x {info.ncols})")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "px/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "scale": args.scale, "sample_scale": scale},
+        "config": {"workload": WORKLOAD, "scale": args.scale, "polygons": w.table.n_geoms,
+                   "vertices": w.table.n_vertices, "raster": [info.nrows, info.ncols]},
         "edges_per_s": edges / (ms / 1e3),
-        "cpu_baseline": {"value": value, "unit": "px/s", "cores": 2, "kind": "port",
-                         "sample": f"per step {what}: the two burns (sum, count) run in 2 host threads, "
+        "cpu_baseline": {"value": value, "unit": "px/s", "cores": REF_THREADS, "kind": "port",
+                         "sample": f"the full workload every step ({w.table.n_geoms} polygons, {info.nrows} x "
+                                   f"{info.ncols}): the two burns (sum f64, count u32) in {REF_THREADS} host threads, "
                                    "each single-threaded like the reference's single-band process loop"},
         "e2e": {"value": value, "unit": "px/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def _roofline(ms, alg_step, nv, ng, acc, phase, hbm, args, peaks) -> dict:
+    """Whole-step roofline (frac) and per-phase figures.
+
+    frac = algorithmic bytes of the step / ms_per_step / measured HBM peak.
+    Each phase is charged the algorithmic bytes it moves for the first time:
+    the span kernels read the vertex table (16 B per vertex and call), the
+    fill writes the rasters and reads the field values; prep re-reads the
+    vertices (counted as traffic, not as algorithmic bytes) and the bucket
+    phase only moves the engine's own coverage records."""
+    out_bytes = acc[0][0]["out_bytes"] + acc[0][1]["out_bytes"]
+    charged = {"ms_prep": 0, "ms_spans": 2 * 16 * nv, "ms_bucket": 0, "ms_fill": out_bytes + 8 * ng}
+    kernels = {
+        "ms_prep": "k_validate, k_part_geom, k_part_prep, scans, k_part_lists",
+        "ms_spans": "k_poly_spans_narrow, k_poly_spans, k_line_spans, k_point_spans",
+        "ms_bucket": "bucket scan, k_scatter",
+        "ms_fill": "k_fill_warp, k_fill_big, k_fill_depth",
+    }
+    per_phase = {}
+    for k, t in phase.items():
+        gbs = charged[k] / (t / 1e3) / 1e9 if t > 0 else None
+        per_phase[k[3:]] = {"kernels": kernels[k], "ms_per_step": t, "algorithmic_bytes": charged[k],
+                            "gbs": gbs, "frac": gbs / hbm if gbs is not None else None}
+    dom = max(per_phase, key=lambda k: per_phase[k]["ms_per_step"])
+    achieved = alg_step / (ms / 1e3) / 1e9
+    # DRAM bytes per step of every kernel from one-kernel ncu captures
+    # (profiles/dram_traffic.json), when the workload matches
+    traffic, traffic_src = None, None
+    tpath = ROOT / "profiles" / "dram_traffic.json"
+    if tpath.exists():
+        t = json.loads(tpath.read_text())
+        if t.get("workload") == WORKLOAD and float(t.get("scale", -1)) == float(args.scale):
+            traffic = t.get("bytes_per_step")
+            traffic_src = t.get("source")
+    return {"bound": "hbm", "scope": "whole step (both calls)", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "target_frac": 0.60, "algorithmic_bytes_per_step": alg_step,
+            "traffic": traffic, "traffic_source": traffic_src,
+            "traffic_over_algorithmic": (traffic / alg_step) if traffic else None,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if not peaks.get("fallback") else "fallback",
+            "dominant_phase": dom, "phases": per_phase,
+            "records_per_step": acc[0][0]["spans"] + acc[0][1]["spans"]}
 
 
 def run_gb300(args) -> None:
@@ -239,14 +273,13 @@ def run_gb300(args) -> None:
     launches = sum(s1["kernel_launches"] + s2["kernel_launches"] for s1, s2 in acc)
     phase = {k: float(np.mean([s1[k] + s2[k] for s1, s2 in acc]))
              for k in ("ms_prep", "ms_spans", "ms_bucket", "ms_fill")}
-    # algorithmic bytes of one step's phases (both calls):
-    #   fill  : the dense rasters written + every coverage record read (8 B)
-    #           + the gathered f64 value of each record of the sum call (8 B)
-    #   spans : the vertex table read (16 B per vertex and call) + every
-    #           coverage record written (wid, part, mask: 12 B)
-    recs_sum, recs_cnt = acc[0][0]["spans"], acc[0][1]["spans"]
-    fill_bytes = acc[0][0]["out_bytes"] + acc[0][1]["out_bytes"] + 8 * (recs_sum + recs_cnt) + 8 * recs_sum
-    span_bytes = 2 * 16 * w.table.n_vertices + 12 * (recs_sum + recs_cnt)
+    # algorithmic bytes of one step (both calls), the per-job figure of the
+    # measurement plan: 16 B per vertex (f64 x, y) + the field values read
+    # + every output pixel written once (background included)
+    nv, ng = w.table.n_vertices, w.table.n_geoms
+    alg_sum = 16 * nv + 8 * ng + acc[0][0]["out_bytes"]
+    alg_cnt = 16 * nv + acc[0][1]["out_bytes"]  # count burns T::one(): no field read
+    alg_step = alg_sum + alg_cnt
     # the slowest rank's step time; the pixel writes of every rank (each burns
     # its own job: seed + rank)
     dev = torch.device("cuda", local)
@@ -272,11 +305,16 @@ def run_gb300(args) -> None:
         o_sum = pinned(np.empty((1, info.nrows, info.ncols), np.float64), fill=False)
         o_cnt = pinned(np.empty((1, info.nrows, info.ncols), np.uint32), fill=False)
 
-        def host_step():
+        e_stats: list = []
+
+        def host_step(keep=False):
+            s1, s2 = {}, {}
             rz.rasterize_table(ptab, info, values=pvals, fn="sum", background=np.nan, dtype="float64", out=o_sum,
-                               context=ctx)
+                               context=ctx, stats=s1)
             rz.rasterize_table(ptab, info, values=None, fn="count", background=0, dtype="uint32", out=o_cnt,
-                               context=ctx)
+                               context=ctx, stats=s2)
+            if keep:
+                e_stats.append((s1, s2))
 
         host_step()
         barrier()
@@ -284,48 +322,39 @@ def run_gb300(args) -> None:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.e2e_steps):
-            host_step()
+            host_step(keep=True)
         e1.record(stream)
         torch.cuda.synchronize()
         e_ms = max_over_ranks(e0.elapsed_time(e1) / args.e2e_steps, device=dev)
         h2d = sum(a.nbytes for a in (tb.part_offsets, tb.part_kind, tb.ring_offsets, tb.vertex_offsets, tb.xy))
         h2d = 2 * h2d + w.values.nbytes
+        d2h = o_sum.nbytes + o_cnt.nbytes
+        # the engine's own events: host->device copies before the prep, and
+        # the device->host tail after the last fill (copies that overlap the
+        # fill are inside ms_fill)
+        ms_h2d = float(np.mean([a["ms_h2d"] + b["ms_h2d"] for a, b in e_stats]))
+        ms_d2h = float(np.mean([a["ms_d2h"] + b["ms_d2h"] for a, b in e_stats]))
+        ms_dev = float(np.mean([a["ms_device_total"] + b["ms_device_total"] for a, b in e_stats]))
         e2e = {"value": px_all / (e_ms / 1e3), "unit": "px/s", "ms_per_step": e_ms,
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(o_sum.nbytes + o_cnt.nbytes)}
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_h2d_per_step": ms_h2d, "ms_d2h_tail_per_step": ms_d2h, "ms_engine_per_step": ms_dev,
+               "h2d_gbs": h2d / (ms_h2d / 1e3) / 1e9 if ms_h2d > 0 else None,
+               "host_link_gbs": (h2d + d2h) / (e_ms / 1e3) / 1e9,
+               "buffers": "pinned host memory (torch pin_memory)"}
 
     peaks = _measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    # dominant kernel phase: the larger of span generation and fill
-    phases = {"spans": ("span generation (k_poly_spans_narrow, k_poly_spans)", phase["ms_spans"], span_bytes),
-              "fill": ("fill (k_fill_warp, k_fill_big, k_fill_depth)", phase["ms_fill"], fill_bytes)}
-    dom_key = max(phases, key=lambda k: phases[k][1])
-    dom, dom_ms, dom_bytes = phases[dom_key]
-    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
-    # DRAM bytes per step of the dominant phase from the ncu capture of this
-    # workload (profiles/dram_traffic.json), when the workload matches
-    traffic, traffic_src = None, None
-    tpath = ROOT / "profiles" / "dram_traffic.json"
-    if tpath.exists():
-        t = json.loads(tpath.read_text())
-        if t.get("workload") == WORKLOAD and float(t.get("scale", -1)) == float(args.scale):
-            traffic = t["phases"].get(dom_key, {}).get("bytes")
-            traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum per step, profiles/dram_traffic.json"
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": traffic, "traffic_source": traffic_src,
-                "traffic_over_algorithmic": (traffic / dom_bytes) if traffic else None,
-                "peak_source": "measured" if not peaks.get("fallback") else "fallback",
-                "algorithmic_bytes_per_step": {"spans": span_bytes, "fill": fill_bytes},
-                "gbs_per_phase": {k: v[2] / (v[1] / 1e3) / 1e9 for k, v in phases.items()},
-                "phase_ms": phase}
+    roofline = _roofline(ms, alg_step, nv, ng, acc, phase, hbm, args, peaks)
 
     batched = _batched_leg(args, ctx, local) if (world == 1 and args.batch_jobs > 0) else None
     served = _served_leg(args, local) if (world == 1 and args.serve_seconds > 0) else None
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_baseline:
-        s, cpx, _ = _oracle_step(w, info, threads=1)
-        cpu = {"value": cpx / s, "unit": "px/s", "cores": 1, "kind": "port",
-               "sample": "full workload (sum f64 + count u32), one host thread, oracle/ restatement"}
+        s, cpx, _ = _oracle_step(w, info, threads=REF_THREADS)
+        cpu = {"value": cpx / s, "unit": "px/s", "cores": REF_THREADS, "kind": "port",
+               "sample": f"one step of the full workload (sum f64 + count u32) in {REF_THREADS} host threads, "
+                         "one per burn, oracle/ restatement"}
 
     if rank == 0:
         line = {
@@ -416,9 +445,10 @@ def _served_leg(args, local) -> dict:
     """A served stream: Poisson arrivals drawn from a pool of uneven jobs
     (sides log-uniform 256-16384, float32 and uint8 outputs) whose geometry
     is resident on the device, for `serve_seconds` per rate.  The batching
-    server (two streams, 120 GB admission budget) against the same server
-    with one job per call on one stream (the plain path).  Each result is
-    released as soon as it completes."""
+    server (two streams, `serve_budget_gb` admission budget) against the same
+    server with one job per call on one stream (the plain path), at every
+    rate up to `serve_plain_max_rate`.  Each result is released as soon as it
+    completes.  px/s counts the raster pixels of the completed jobs."""
     import torch
 
     import rusterize_gb300 as rz
@@ -442,6 +472,7 @@ def _served_leg(args, local) -> dict:
     def run(rate, batched):
         rng = np.random.default_rng(int(rate) * 7 + batched)
         lat, errors, lock = [], [], threading.Lock()
+        px_done = [0]
         done = threading.Event()
         n_sub = [0]
 
@@ -455,6 +486,7 @@ def _served_leg(args, local) -> dict:
             with lock:
                 if r is not None:
                     lat.append(r.latency)
+                    px_done[0] += f.px
                 finished = len(lat) + len(errors) == n_sub[0] and closed[0]
             if r is not None:
                 r.release()
@@ -477,7 +509,9 @@ def _served_leg(args, local) -> dict:
                 job, dtype = pool[int(rng.integers(0, len(pool)))]
                 with lock:
                     n_sub[0] += 1
-                srv.submit(job, dtype=dtype).add_done_callback(on_done)
+                fut = srv.submit(job, dtype=dtype)
+                fut.px = job.info.nrows * job.info.ncols
+                fut.add_done_callback(on_done)
             with lock:
                 closed[0] = True
                 if len(lat) + len(errors) == n_sub[0]:
@@ -491,7 +525,7 @@ def _served_leg(args, local) -> dict:
         if errors:
             print(f"served leg: {len(errors)} failed requests, first: {errors[0]}", file=sys.stderr)
         return {"submitted": n_sub[0], "completed": len(lat), "failed": len(errors),
-                "jobs_per_s": len(lat) / (t_end - t0),
+                "jobs_per_s": len(lat) / (t_end - t0), "px_per_s": px_done[0] / (t_end - t0),
                 "p50_ms": float(np.percentile(a, 50)) if len(a) else None,
                 "p99_ms": float(np.percentile(a, 99)) if len(a) else None, "batches": batches,
                 "drain_s": t_end - t0 - args.serve_seconds}

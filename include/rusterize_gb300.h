@@ -279,10 +279,15 @@ void* rz_context_stream(rz_context* ctx);
  * caller's back, and plugin hosts (a database or GIS engine with its own pool
  * allocator) that own every allocation.  Same arguments and results as
  * rz_rasterize, except:
- *   - no context: work goes to `stream` (a cudaStream_t, NULL = default);
+ *   - no context: work goes to `stream` (a cudaStream_t, NULL = the legacy
+ *     default stream), which must belong to the current device
+ *     (RZ_INVALID_ARGUMENT otherwise);
  *   - the geometry arrays, per-geometry values, band_of_geom and `out` are
- *     DEVICE pointers (xy 16-byte aligned); a scalar value (with
- *     RZ_FLAG_SCALAR_VALUE) and the background are host values;
+ *     DEVICE pointers (xy 16-byte aligned) holding the counts given in `g`;
+ *     their offsets are validated on the device (RZ_INVALID_ARGUMENT), but
+ *     arrays shorter than their counts cannot be detected; a scalar value
+ *     (with RZ_FLAG_SCALAR_VALUE) and the background are host values, and a
+ *     NULL background is zero, as in rz_rasterize;
  *   - all scratch comes from one static device array of
  *     RZ_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library
  *     until the process exits; a job whose tables, buckets or spans do not

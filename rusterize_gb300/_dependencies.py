@@ -1,69 +1,84 @@
-"""Optional third-party modules, imported only when present.
+"""Optional third-party libraries of the Python front end.
 
-Same contract as the reference's python/python/rusterize/_dependencies.py:
-each name is either the real module or a placeholder that raises
-ModuleNotFoundError on attribute access, plus availability predicates.
+The front end accepts GeoPandas and polars-st inputs and can return xarray
+rasters or polars frames, but it burns without any of those libraries.  Each
+one is represented here by an ``OptionalModule``: a proxy that imports the
+library the first time one of its attributes is used, and raises
+ModuleNotFoundError naming the library when it is not installed.  The
+predicates below tell the front end which input types can occur and which
+encodings can be produced, without importing anything.
 """
 
 from __future__ import annotations
 
+import importlib
 import importlib.util
-import sys
-from functools import cache
 from typing import Any
 
 
-class _Missing:
+class OptionalModule:
+    """Stand-in for an importable-if-installed module."""
+
+    __slots__ = ("_name", "_installed", "_module")
+
     def __init__(self, name: str):
         self._name = name
+        self._installed: bool | None = None
+        self._module = None
+
+    @property
+    def installed(self) -> bool:
+        if self._installed is None:
+            try:
+                self._installed = importlib.util.find_spec(self._name) is not None
+            except (ImportError, ValueError):
+                self._installed = False
+        return self._installed
+
+    def load(self, what: str = "") -> Any:
+        """The module itself, imported on first use."""
+        if self._module is None:
+            if not self.installed:
+                need = f" (needed for {self._name}.{what})" if what else ""
+                raise ModuleNotFoundError(f"the optional dependency {self._name!r} is not installed{need}",
+                                          name=self._name)
+            self._module = importlib.import_module(self._name)
+        return self._module
 
     def __getattr__(self, attr: str) -> Any:
-        raise ModuleNotFoundError(f"{attr} requires the {self._name!r} module to be installed.")
+        return getattr(self.load(attr), attr)
 
 
-def _optional(name: str) -> tuple[Any, bool]:
-    if name in sys.modules:
-        return sys.modules[name], True
-    try:
-        spec = importlib.util.find_spec(name)
-    except (ModuleNotFoundError, ValueError):
-        spec = None
-    if spec is None or spec.loader is None:
-        return _Missing(name), False
-    spec.loader = importlib.util.LazyLoader(spec.loader)
-    module = importlib.util.module_from_spec(spec)
-    sys.modules[name] = module
-    spec.loader.exec_module(module)
-    return module, True
-
-
-geopandas, GEOPANDAS_AVAILABLE = _optional("geopandas")
-polars, POLARS_AVAILABLE = _optional("polars")
-polars_st, POLARS_ST_AVAILABLE = _optional("polars_st")
-xarray, XARRAY_AVAILABLE = _optional("xarray")
-_rioxarray, RIOXARRAY_AVAILABLE = _optional("rioxarray")
-shapely, SHAPELY_AVAILABLE = _optional("shapely")
+geopandas = OptionalModule("geopandas")
+polars = OptionalModule("polars")
+polars_st = OptionalModule("polars_st")
+xarray = OptionalModule("xarray")
+rioxarray = OptionalModule("rioxarray")
+shapely = OptionalModule("shapely")
 
 
 def _xarray_available() -> bool:
-    return XARRAY_AVAILABLE and RIOXARRAY_AVAILABLE
+    """encoding="xarray" needs xarray and the rioxarray accessor (for the CRS)."""
+    return xarray.installed and rioxarray.installed
 
 
 def _polars_available() -> bool:
-    return POLARS_AVAILABLE
+    return polars.installed
 
 
-@cache
-def _mro_mentions(cls: type, module: str) -> bool:
-    try:
-        return any(f"{module}." in str(o) for o in cls.mro())
-    except TypeError:
-        return False
+def _class_from(obj: Any, package: str) -> bool:
+    """Whether the type of obj, or one of its bases, is defined in `package`."""
+    for cls in type(obj).__mro__:
+        mod = getattr(cls, "__module__", "") or ""
+        if mod == package or mod.startswith(package + "."):
+            return True
+    return False
 
 
 def _check_for_geopandas(obj: Any) -> bool:
-    return GEOPANDAS_AVAILABLE and _mro_mentions(type(obj), "geopandas")
+    return geopandas.installed and _class_from(obj, "geopandas")
 
 
 def _check_for_polars_st(obj: Any) -> bool:
-    return POLARS_ST_AVAILABLE and _mro_mentions(type(obj), "polars")
+    """A polars frame (polars-st keeps its geometries in polars frames)."""
+    return polars_st.installed and _class_from(obj, "polars")

@@ -8,13 +8,14 @@ the GB300 engine through its C ABI.
 
 from __future__ import annotations
 
+import math
 import operator
 from typing import Any
 
 import numpy as np
 
 from . import _lib
-from ._dependencies import SHAPELY_AVAILABLE, shapely
+from ._dependencies import shapely
 from ._lib import PanicException
 from .engine import RasterInfo, raster_info, rasterize_table, rasterize_table_sparse
 from .geometry import GeometryTable, from_wkb, from_wkt
@@ -50,7 +51,7 @@ def parse_geometry(obj: Any) -> GeometryTable:
 
 def _to_wkb(obj: Any) -> list[bytes]:
     # shapely >= 2 (parse_geometry.rs:90-107)
-    if not SHAPELY_AVAILABLE:
+    if not shapely.installed:
         raise ModuleNotFoundError("shapely must be installed to rasterize shapely geometries")
     if not str(shapely.__version__).startswith("2"):
         raise ValueError("Shapely version 2 required")
@@ -186,14 +187,38 @@ def _rusterize(geometry: Any, raw_raster_info: dict, pypixel_fn: str, pydf: Any 
     return out
 
 
+def _axis(start: float, end: float, step: float) -> np.ndarray:
+    """ndarray's Array::range(start, end, step): ceil((end - start) / step)
+    elements, element i = start + step * i (one rounding each for the product
+    and the sum, no FMA)."""
+    n = math.ceil((end - start) / step)
+    return start + step * np.arange(max(n, 0), dtype=np.float64)
+
+
+def make_coordinates(info: RasterInfo) -> tuple[np.ndarray, np.ndarray]:
+    """Pixel-centre coordinates (y, x) of the raster: make_coordinates,
+    python/src/geo/raster.rs:45-62 (y descends from ymax - yres / 2)."""
+    y = _axis(info.ymax - info.yres / 2.0, info.ymax - float(info.nrows) * info.yres, -info.yres)
+    x = _axis(info.xmin + info.xres / 2.0, info.xmin + float(info.ncols) * info.xres, info.xres)
+    return y, x
+
+
 def _to_xarray(data: np.ndarray, info: RasterInfo, band_names: list[str]):
-    """python/src/encoding/xarray.rs:10-58 with coordinates at pixel centres
-    (python/src/geo/raster.rs:45-62)."""
+    """build_xarray (python/src/encoding/xarray.rs:10-58): a DataArray with
+    dims (bands, y, x), built with DataArray.from_dict from the same
+    dictionary, and the EPSG code written as its CRS by rioxarray."""
+    from ._dependencies import rioxarray
     from ._dependencies import xarray as xr
 
-    y = np.arange(info.ymax - info.yres / 2.0, info.ymax - info.nrows * info.yres, -info.yres)[: info.nrows]
-    x = np.arange(info.xmin + info.xres / 2.0, info.xmin + info.ncols * info.xres, info.xres)[: info.ncols]
-    da = xr.DataArray(data, dims=("band", "y", "x"), coords={"band": band_names, "y": y, "x": x})
+    rioxarray.load()  # registers the .rio accessor
+    y, x = make_coordinates(info)
+    spec = {
+        "data": data,
+        "dims": ["bands", "y", "x"],
+        "coords": {"x": {"dims": "x", "data": x}, "y": {"dims": "y", "data": y},
+                   "bands": {"dims": "bands", "data": list(band_names)}},
+    }
+    da = xr.DataArray.from_dict(spec)
     if info.epsg is not None:
-        da = da.rio.write_crs(f"EPSG:{info.epsg}")
+        da = da.rio.write_crs(info.epsg)
     return da

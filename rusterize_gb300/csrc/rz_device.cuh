@@ -52,9 +52,6 @@ constexpr int SMALL_SMEM = SMALL_WARPS * SMALL_WARP_SMEM;
 // BIG_CAP records of one word at a time.
 constexpr int FILL_WARP_MAX = 64;    // records held in registers (two per lane)
 constexpr int FILL_WARP_SORT = 256;  // records sorted in shared memory by one warp
-// Bytes of record scratch per record: 12 before the scatter, 8 after it and
-// 8 for its value.
-constexpr size_t RECORD_BYTES = 28;
 constexpr int BIG_CAP = 1024;
 
 // Longest Bresenham walk one thread performs for a single segment.

@@ -17,6 +17,7 @@
 #include "rz_device.cuh"
 #include "rz_fill.cuh"
 #include "rz_internal.h"
+#include "rz_layout.h"
 #include "rz_kernels.cuh"
 #include "rz_scan.cuh"
 #include "rz_sort.cuh"
@@ -481,10 +482,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   const size_t o_ctrl = L.take(sizeof(Ctrl));
   RZ_CUDA(ensure(ctx->main, L.off));
   if (!out_dev && !sp) RZ_CUDA(ensure(ctx->out, out_elems * tsize));
-  unsigned long long cap = std::max<unsigned long long>(ctx->span_cap_hint, 2 * V + (1ull << 20));
-  if (cap > 0xFFFFFFF0ull) cap = 0xFFFFFFF0ull;
-  RZ_CUDA(ensure(ctx->spans, RECORD_BYTES * cap + 16));
-  cap = std::min<unsigned long long>((ctx->spans.cap - 16) / RECORD_BYTES, 0xFFFFFFF0ull) & ~1ull;
+  unsigned long long cap = rzl::record_cap_request(std::max<unsigned long long>(ctx->span_cap_hint, 2 * V + (1ull << 20)));
 
   char* mb = static_cast<char*>(ctx->main.p);
   auto at = [&](size_t o) { return static_cast<void*>(mb + o); };
@@ -560,17 +558,19 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   const fill_fn fill = fill_for(dt);
   unsigned reruns = 0;
   while (true) {
-    cap &= ~1ull;  // keeps the sorted {part, xs} array 8-byte aligned
-    RZ_CUDA(ensure(ctx->spans, RECORD_BYTES * cap + 16));
+    RZ_CUDA(ensure(ctx->spans, rzl::record_bytes_for(cap)));
+    const rzl::RecordLayout RL = rzl::record_layout(ctx->spans.cap);  // the whole buffer: cap or more
+    cap = RL.cap;
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[7], s));
+    char* rbase = static_cast<char*>(ctx->spans.p);
     RecBuf sb;
     sb.cap = cap;
     sb.nbuckets = nbuckets;
-    sb.wid = static_cast<unsigned*>(ctx->spans.p);
-    sb.part = sb.wid + cap;
-    sb.mask = sb.part + cap;
-    uint2* sorted = reinterpret_cast<uint2*>(sb.mask + cap);
-    void* rvals = sorted + cap;
+    sb.wid = reinterpret_cast<unsigned*>(rbase + RL.off_wid);
+    sb.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
+    sb.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
+    uint2* sorted = reinterpret_cast<uint2*>(rbase + RL.off_sorted);
+    void* rvals = rbase + RL.off_rvals;
     k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
     RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
     launches += 1;
@@ -613,13 +613,8 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     const Ctrl& hc = *ctx->h_ctrl;
     if (hc.err) return ctrl_error(hc, err, errlen);
     if (hc.span_count > cap) {
-      unsigned long long want = hc.span_count + hc.span_count / 4 + 1024;
-      if (want > 0xFFFFFFF0ull) {
-        if (hc.span_count > 0xFFFFFFF0ull)
-          return fail(err, errlen, RZ_VALUE_ERROR, "more than 2^32 spans in one call");
-        want = 0xFFFFFFF0ull;
-      }
-      cap = want;
+      cap = rzl::record_cap_regrow(hc.span_count);
+      if (cap == 0) return fail(err, errlen, RZ_VALUE_ERROR, "more than 2^32 coverage records in one call");
       ++reruns;
       continue;
     }
@@ -636,12 +631,14 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   if (sp) {
     // ---- sparse: order the records by (band, part, row, word), expand ----
     const unsigned long long n = ctx->h_ctrl->span_count;
+    const rzl::RecordLayout RL = rzl::record_layout(ctx->spans.cap);
+    char* rbase = static_cast<char*>(ctx->spans.p);
     RecBuf sbr;
     sbr.cap = cap;
     sbr.nbuckets = nbuckets;
-    sbr.wid = static_cast<unsigned*>(ctx->spans.p);
-    sbr.part = sbr.wid + cap;
-    sbr.mask = sbr.part + cap;
+    sbr.wid = reinterpret_cast<unsigned*>(rbase + RL.off_wid);
+    sbr.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
+    sbr.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
     const unsigned long long nsort = std::max<unsigned long long>(n, nb > 1 ? P : 0);
     Layout SL;
     const size_t o_k0 = SL.take(8 * (nsort ? nsort : 1)), o_k1 = SL.take(8 * (nsort ? nsort : 1));
@@ -856,7 +853,7 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
                               size_t errlen) {
   rz::clear_err(err, errlen);
   if (stats) std::memset(stats, 0, sizeof(*stats));
-  if (!g || !info || !background || !out) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null argument");
+  if (!g || !info || !out) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null argument");
   const size_t tsize = rz_dtype_size(dt);
   if (tsize == 0) return fail(err, errlen, RZ_VALUE_ERROR, "Unsupported dtype");
   if ((int)fn < 0 || (int)fn > 6) return fail(err, errlen, RZ_VALUE_ERROR, "Unknown pixel function");
@@ -876,7 +873,7 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   if (reinterpret_cast<uintptr_t>(g->xy) & 15)
     return fail(err, errlen, RZ_INVALID_ARGUMENT, "device xy must be 16-byte aligned");
   unsigned long long bg_bits = 0, scalar_bits = one_bits(dt);
-  std::memcpy(&bg_bits, background, tsize);
+  if (background) std::memcpy(&bg_bits, background, tsize);  // NULL: a zero background, as rz_rasterize
   const bool per_geom_values = values && !(flags & RZ_FLAG_SCALAR_VALUE);
   if (values && (flags & RZ_FLAG_SCALAR_VALUE)) {
     scalar_bits = 0;
@@ -902,16 +899,25 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   const size_t o_ctrl = L.take(sizeof(Ctrl));
   const size_t o_spans = L.take(0);
   const size_t min_spans = 1024;
-  if (o_spans + RECORD_BYTES * min_spans + 16 > RZ_NOALLOC_SCRATCH_BYTES)
+  if (o_spans + rzl::record_bytes_for(min_spans) > RZ_NOALLOC_SCRATCH_BYTES)
     return fail(err, errlen, RZ_VALUE_ERROR,
                 "job needs %zu bytes of scratch before any span; the allocation-free entry point is limited to "
                 "%zu bytes (use rz_rasterize)",
-                o_spans + RECORD_BYTES * min_spans + 16, (size_t)RZ_NOALLOC_SCRATCH_BYTES);
-  unsigned long long cap = ((RZ_NOALLOC_SCRATCH_BYTES - o_spans - 16) / RECORD_BYTES) & ~1ull;
-  if (cap > 0xFFFFFFF0ull) cap = 0xFFFFFFF0ull;
+                (size_t)(o_spans + rzl::record_bytes_for(min_spans)), (size_t)RZ_NOALLOC_SCRATCH_BYTES);
+  const rzl::RecordLayout RL = rzl::record_layout(RZ_NOALLOC_SCRATCH_BYTES - o_spans);
+  const unsigned long long cap = RL.cap;
 
   int dev = 0;
   RZ_CUDA(cudaGetDevice(&dev));
+  if (stream) {
+    // the static array used is the current device's: the stream must be on it
+    int sdev = -1;
+    RZ_CUDA(cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev));
+    if (sdev != dev)
+      return fail(err, errlen, RZ_INVALID_ARGUMENT,
+                  "stream belongs to device %d but device %d is current; make the stream's device current", sdev,
+                  dev);
+  }
   if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(err, errlen, RZ_NO_DEVICE, "device %d unsupported", dev);
   NoAllocDevice nd;
   {
@@ -983,14 +989,15 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   pt.last_kept = last_kept;
   launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sms, s);
   RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
+  char* rbase = static_cast<char*>(at(o_spans));
   RecBuf sb;
   sb.cap = cap;
   sb.nbuckets = nbuckets;
-  sb.wid = static_cast<unsigned*>(at(o_spans));
-  sb.part = sb.wid + cap;
-  sb.mask = sb.part + cap;
-  uint2* sorted = reinterpret_cast<uint2*>(sb.mask + cap);
-  void* rvals = sorted + cap;
+  sb.wid = reinterpret_cast<unsigned*>(rbase + RL.off_wid);
+  sb.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
+  sb.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
+  uint2* sorted = reinterpret_cast<uint2*>(rbase + RL.off_sorted);
+  void* rvals = rbase + RL.off_rvals;
   k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
   RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
   ++launches;
@@ -1305,21 +1312,22 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
   unsigned char* gctr = static_cast<unsigned char*>(at(o_gctr));
   const fill_fn fill = fill_for(dt);
 
-  unsigned long long cap = std::max<unsigned long long>(ctx->span_cap_hint, 2 * Vt + (1ull << 20));
-  if (cap > 0xFFFFFFF0ull) cap = 0xFFFFFFF0ull;
+  unsigned long long cap =
+      rzl::record_cap_request(std::max<unsigned long long>(ctx->span_cap_hint, 2 * Vt + (1ull << 20)));
   unsigned reruns = 0;
   while (true) {
-    cap &= ~1ull;
-    RZ_CUDA(ensure(ctx->spans, RECORD_BYTES * cap + 16));
-    cap = std::min<unsigned long long>(cap, (ctx->spans.cap - 16) / RECORD_BYTES) & ~1ull;
+    RZ_CUDA(ensure(ctx->spans, rzl::record_bytes_for(cap)));
+    const rzl::RecordLayout RL = rzl::record_layout(ctx->spans.cap);
+    cap = RL.cap;
+    char* rbase = static_cast<char*>(ctx->spans.p);
     RecBuf sb;
     sb.cap = cap;
     sb.nbuckets = nbuckets;
-    sb.wid = static_cast<unsigned*>(ctx->spans.p);
-    sb.part = sb.wid + cap;
-    sb.mask = sb.part + cap;
-    uint2* sorted = reinterpret_cast<uint2*>(sb.mask + cap);
-    void* rvals = sorted + cap;
+    sb.wid = reinterpret_cast<unsigned*>(rbase + RL.off_wid);
+    sb.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
+    sb.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
+    uint2* sorted = reinterpret_cast<uint2*>(rbase + RL.off_sorted);
+    void* rvals = rbase + RL.off_rvals;
     k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
     RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * (nbuckets ? nbuckets : 1), s));
     RZ_CUDA(cudaMemsetAsync(gctr, 0, 16 * (n + 1), s));
@@ -1369,13 +1377,8 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
     if (hc.err == ERR_BAD_JOB && hc.err_index < n) hc.err_index = wave[hc.err_index].idx;  // the caller's index
     if (hc.err) return ctrl_error(hc, err, errlen);
     if (hc.span_count > cap) {
-      unsigned long long want = hc.span_count + hc.span_count / 4 + 1024;
-      if (want > 0xFFFFFFF0ull) {
-        if (hc.span_count > 0xFFFFFFF0ull)
-          return fail(err, errlen, RZ_VALUE_ERROR, "more than 2^32 coverage records in one wave");
-        want = 0xFFFFFFF0ull;
-      }
-      cap = want;
+      cap = rzl::record_cap_regrow(hc.span_count);
+      if (cap == 0) return fail(err, errlen, RZ_VALUE_ERROR, "more than 2^32 coverage records in one wave");
       ++reruns;
       continue;
     }

@@ -6,8 +6,11 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "rz_internal.h"
@@ -285,19 +288,31 @@ namespace {
 struct ChunkResult {
   GeomTable t;
   size_t fail_item = SIZE_MAX;
+  bool out_of_memory = false;  // the chunk's table could not grow
   std::string msg;
 };
 
-// parse_one(k, table, msg) -> 1: parsed and kept, 0: parsed and dropped, -1: error
+// parse_one(k, table, msg) -> 1: parsed and kept, 0: parsed and dropped, -1: error.
+// Runs on a worker thread: nothing may escape it (an exception leaving a
+// std::thread ends the process), so allocation failures are recorded.
 template <typename ParseOne>
 void parse_chunk(size_t k0, size_t k1, ChunkResult& c, ParseOne&& parse_one) {
-  for (size_t k = k0; k < k1; ++k) {
-    const int r = parse_one(k, c.t, c.msg);
-    if (r < 0) {
-      c.fail_item = k;
-      return;
+  size_t k = k0;
+  try {
+    for (; k < k1; ++k) {
+      const int r = parse_one(k, c.t, c.msg);
+      if (r < 0) {
+        c.fail_item = k;
+        return;
+      }
+      if (r > 0) c.t.part_offsets.push_back(c.t.part_kind.size());
     }
-    if (r > 0) c.t.part_offsets.push_back(c.t.part_kind.size());
+  } catch (const std::bad_alloc&) {
+    c.fail_item = k;
+    c.out_of_memory = true;
+  } catch (...) {
+    c.fail_item = k;
+    c.msg = "internal error while parsing";
   }
 }
 
@@ -326,8 +341,8 @@ unsigned parse_threads(size_t n, size_t bytes) {
 }
 
 template <typename ParseOne>
-rz_status parse_all(size_t n, size_t bytes, rz_geom_buffer** out, ParseOne&& parse_one, const char* what,
-                    char* err, size_t errlen) {
+rz_status parse_all_impl(size_t n, size_t bytes, rz_geom_buffer** out, ParseOne&& parse_one, const char* what,
+                         char* err, size_t errlen) {
   const unsigned T = parse_threads(n, bytes);
   std::vector<ChunkResult> chunks(T);
   if (T == 1) {
@@ -335,14 +350,22 @@ rz_status parse_all(size_t n, size_t bytes, rz_geom_buffer** out, ParseOne&& par
   } else {
     std::vector<std::thread> ts;
     ts.reserve(T);
-    for (unsigned c = 0; c < T; ++c) {
-      const size_t k0 = n * c / T, k1 = n * (c + 1) / T;
-      ts.emplace_back([&, c, k0, k1] { parse_chunk(k0, k1, chunks[c], parse_one); });
+    try {
+      for (unsigned c = 0; c < T; ++c) {
+        const size_t k0 = n * c / T, k1 = n * (c + 1) / T;
+        ts.emplace_back([&, c, k0, k1] { parse_chunk(k0, k1, chunks[c], parse_one); });
+      }
+    } catch (...) {  // a thread could not start: finish the started ones before reporting
+      for (auto& th : ts) th.join();
+      throw;
     }
     for (auto& th : ts) th.join();
   }
   for (const ChunkResult& c : chunks)  // chunks are in item order: the first failure is the first reported
-    if (c.fail_item != SIZE_MAX)
+    if (c.fail_item != SIZE_MAX && c.out_of_memory)
+      return fail(err, errlen, RZ_OUT_OF_MEMORY, "out of host memory while parsing geometry (item %zu)",
+                  c.fail_item);
+    else if (c.fail_item != SIZE_MAX)
       return fail(err, errlen, RZ_PARSE_ERROR, "Cannot parse geometry. Check that the %s valid. (item %zu%s%s)",
                   what, c.fail_item, c.msg.empty() ? "" : ": ", c.msg.c_str());
   auto* buf = new rz_geom_buffer();
@@ -371,6 +394,20 @@ rz_status parse_all(size_t n, size_t bytes, rz_geom_buffer** out, ParseOne&& par
   }
   *out = buf;
   return RZ_OK;
+}
+
+// The same, with allocation failures of the merge (and of thread creation)
+// turned into a status: no exception crosses the C boundary.
+template <typename ParseOne>
+rz_status parse_all(size_t n, size_t bytes, rz_geom_buffer** out, ParseOne&& parse_one, const char* what,
+                    char* err, size_t errlen) {
+  try {
+    return parse_all_impl(n, bytes, out, std::forward<ParseOne>(parse_one), what, err, errlen);
+  } catch (const std::bad_alloc&) {
+    return fail(err, errlen, RZ_OUT_OF_MEMORY, "out of host memory while parsing geometry");
+  } catch (const std::exception& e) {
+    return fail(err, errlen, RZ_RUNTIME_ERROR, "geometry parsing failed: %s", e.what());
+  }
 }
 
 }  // namespace

@@ -73,16 +73,21 @@ class GeometryTable:
 
     def select(self, idx: Sequence[int]) -> "GeometryTable":
         """Sub-table of the given geometries (in the given order)."""
-        b = TableBuilder()
-        for gi in idx:
-            for p in range(int(self.part_offsets[gi]), int(self.part_offsets[gi + 1])):
-                rings = []
-                for r in range(int(self.ring_offsets[p]), int(self.ring_offsets[p + 1])):
-                    v0, v1 = int(self.vertex_offsets[r]), int(self.vertex_offsets[r + 1])
-                    rings.append((self.xy[v0:v1], int(self.ring_flags[r])))
-                b.add_part(int(self.part_kind[p]), rings)
-            b.end_geometry()
-        return b.build()
+        idx = np.asarray(idx, dtype=np.int64).reshape(-1)
+
+        def ranges(lo: np.ndarray, hi: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+            # the concatenation of arange(lo[i], hi[i]), and the offsets of its pieces
+            n = (hi - lo).astype(np.int64)
+            off = np.concatenate([[0], np.cumsum(n)]).astype(np.int64)
+            flat = np.arange(int(off[-1]), dtype=np.int64) - np.repeat(off[:-1] - lo.astype(np.int64), n)
+            return flat, off
+
+        po, ro, vo = (a.astype(np.int64) for a in (self.part_offsets, self.ring_offsets, self.vertex_offsets))
+        parts, new_po = ranges(po[idx], po[idx + 1])
+        rings, new_ro = ranges(ro[parts], ro[parts + 1])
+        verts, new_vo = ranges(vo[rings], vo[rings + 1])
+        return GeometryTable(new_po.astype(np.uint64), self.part_kind[parts], new_ro.astype(np.uint64),
+                             new_vo.astype(np.uint64), self.ring_flags[rings], self.xy[verts])
 
     @staticmethod
     def concat(tables: Iterable["GeometryTable"]) -> "GeometryTable":

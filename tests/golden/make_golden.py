@@ -1,9 +1,8 @@
 """Generate the golden fixtures of the parity tests from the reference tree.
 
-Run in a container where the reference checkout is mounted (default
-/root/reference, or pass a path):
+Run it with the path of a checkout of the reference:
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py REFERENCE_ROOT
 
 It reads, without executing anything from the reference:
   * python/test/data/standard_output_sum.tif              (uncompressed)
@@ -140,4 +139,6 @@ def main(ref_root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <root of a ttrotto/rusterize checkout>")
+    main(Path(sys.argv[1]))

@@ -1,5 +1,8 @@
 """Full-size checks on the large fill and the mixed collection, through
-properties that hold at any size (the oracle would take minutes there).
+properties that hold at any size.  They add to the bit-exact oracle
+comparisons of test_full_size_oracle.py: each identity pits two GPU paths
+against each other (the ordered fill against the order-free one, write
+order against value order).
 
 Large fill (100,000 polygons, 20,000 x 20,000):
   * `sum` of ones (float64, background 0) equals `count` exactly: every sum
