@@ -15,8 +15,10 @@ into uint32 (background 0).
   cpu_baseline / --impl reference : the CPU restatement of the reference
           (oracle/), timed on this host on the same workload
 
-Multi-GPU (torchrun, N > 1): every rank burns its own independent job
-(seed + rank); no data-path collective ("scaling": "weak").
+Multi-GPU (torchrun, N > 1): by default every rank burns its own
+independent job (seed + rank; "scaling": "weak"); with --shard rows every
+rank burns its row band of the same job from the geometries that can write
+there ("scaling": "strong").  No data-path collective either way.
 """
 
 from __future__ import annotations
@@ -235,19 +237,32 @@ def run_gb300(args) -> None:
     from rusterize_gb300.device import DeviceTable, rasterize_device, upload
 
     ctx = _lib.Context(local)
-    w = _workload(1002 + rank, args.scale)
+    rows_split = args.shard == "rows" and world > 1
+    # replicas: every rank burns its own job (seed + rank); rows: every rank
+    # burns its row band of the same job, from the geometries that can write there
+    w = _workload(1002 + (0 if rows_split else rank), args.scale)
     info = rz.raster_info(w.table, res=w.res, extent=w.extent)
-    dtab = DeviceTable.upload(w.table, device=local)
-    dvals = upload(w.values, device=local)
-    out_sum = torch.empty((1, info.nrows, info.ncols), dtype=torch.float64, device=f"cuda:{local}")
-    out_cnt = torch.empty((1, info.nrows, info.ncols), dtype=torch.int32, device=f"cuda:{local}")
+    rows = None
+    table, values = w.table, w.values
+    if rows_split:
+        from rusterize_gb300.shard import row_bands, select_rows
+
+        rows = row_bands(info.nrows, world)[rank]
+        idx = select_rows(w.table, info, *rows)
+        table, values = w.table.select(idx), w.values[idx]
+    nr = info.nrows if rows is None else rows[1] - rows[0]
+    dtab = DeviceTable.upload(table, device=local)
+    dvals = upload(values, device=local)
+    out_sum = torch.empty((1, nr, info.ncols), dtype=torch.float64, device=f"cuda:{local}")
+    out_cnt = torch.empty((1, nr, info.ncols), dtype=torch.int32, device=f"cuda:{local}")
     stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
 
     def step(stats_acc=None):
         st1, st2 = {}, {}
         rasterize_device(dtab, info, fn="sum", background=np.nan, dtype="float64", values=dvals, out=out_sum,
-                         context=ctx, stats=st1)
-        rasterize_device(dtab, info, fn="count", background=0, dtype="uint32", out=out_cnt, context=ctx, stats=st2)
+                         context=ctx, stats=st1, rows=rows)
+        rasterize_device(dtab, info, fn="count", background=0, dtype="uint32", out=out_cnt, context=ctx, stats=st2,
+                         rows=rows)
         if stats_acc is not None:
             stats_acc.append((st1, st2))
         return st1, st2
@@ -276,7 +291,7 @@ def run_gb300(args) -> None:
     # algorithmic bytes of one step (both calls), the per-job figure of the
     # measurement plan: 16 B per vertex (f64 x, y) + the field values read
     # + every output pixel written once (background included)
-    nv, ng = w.table.n_vertices, w.table.n_geoms
+    nv, ng = table.n_vertices, table.n_geoms
     alg_sum = 16 * nv + 8 * ng + acc[0][0]["out_bytes"]
     alg_cnt = 16 * nv + acc[0][1]["out_bytes"]  # count burns T::one(): no field read
     alg_step = alg_sum + alg_cnt
@@ -298,21 +313,21 @@ def run_gb300(args) -> None:
                 arr[...] = a
             return arr
 
-        tb = w.table
+        tb = table
         ptab = rz.GeometryTable(pinned(tb.part_offsets), pinned(tb.part_kind), pinned(tb.ring_offsets),
                                 pinned(tb.vertex_offsets), pinned(tb.ring_flags), pinned(tb.xy))
-        pvals = pinned(w.values)
-        o_sum = pinned(np.empty((1, info.nrows, info.ncols), np.float64), fill=False)
-        o_cnt = pinned(np.empty((1, info.nrows, info.ncols), np.uint32), fill=False)
+        pvals = pinned(values)
+        o_sum = pinned(np.empty((1, nr, info.ncols), np.float64), fill=False)
+        o_cnt = pinned(np.empty((1, nr, info.ncols), np.uint32), fill=False)
 
         e_stats: list = []
 
         def host_step(keep=False):
             s1, s2 = {}, {}
             rz.rasterize_table(ptab, info, values=pvals, fn="sum", background=np.nan, dtype="float64", out=o_sum,
-                               context=ctx, stats=s1)
+                               context=ctx, stats=s1, rows=rows)
             rz.rasterize_table(ptab, info, values=None, fn="count", background=0, dtype="uint32", out=o_cnt,
-                               context=ctx, stats=s2)
+                               context=ctx, stats=s2, rows=rows)
             if keep:
                 e_stats.append((s1, s2))
 
@@ -327,7 +342,7 @@ def run_gb300(args) -> None:
         torch.cuda.synchronize()
         e_ms = max_over_ranks(e0.elapsed_time(e1) / args.e2e_steps, device=dev)
         h2d = sum(a.nbytes for a in (tb.part_offsets, tb.part_kind, tb.ring_offsets, tb.vertex_offsets, tb.xy))
-        h2d = 2 * h2d + w.values.nbytes
+        h2d = 2 * h2d + values.nbytes
         d2h = o_sum.nbytes + o_cnt.nbytes
         # the engine's own events: host->device copies before the prep, and
         # the device->host tail after the last fill (copies that overlap the
@@ -359,9 +374,11 @@ def run_gb300(args) -> None:
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "px/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "strong" if rows_split else "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "scale": args.scale, "polygons": w.table.n_geoms,
+                       "shard": ("row bands of one job" if rows_split else "one job per rank") if world > 1 else None,
                        "vertices": w.table.n_vertices, "raster": [info.nrows, info.ncols],
                        "l2": "inputs larger than L2 (vertex table and rasters exceed 129 MB); no flush"},
             "edges_per_s": edges_all / (ms / 1e3),
@@ -549,6 +566,8 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--shard", choices=["jobs", "rows"], default="jobs",
+                    help="N > 1: independent jobs per rank (weak scaling) or row bands of one job (strong)")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")

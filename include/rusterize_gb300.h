@@ -192,6 +192,23 @@ rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void* values,
                        const rz_raster_info* info, rz_pixel_fn fn, rz_dtype out_dtype,
                        uint32_t flags, void* out, rz_stats* stats, char* err, size_t errlen);
 
+/* Burn only the rows [row_begin, row_end) of the raster `info` describes
+ * (every band) into `out`, a (bands, row_end - row_begin, ncols) C-order
+ * buffer.  Every pixel decision is taken on the whole raster's grid -- the
+ * world->pixel map, extract_line's bbox filter and the last kept segment,
+ * Bresenham and AllTouched walks, polygon scanlines -- and only the writes
+ * that land in the window are kept, so the result equals the same rows of
+ * rz_rasterize's result bit for bit.  It is the unit of the row-band split of
+ * one job over several GPUs: the reference splits work only across `by`
+ * bands (rust/src/rasterize.rs:88-101); rows of one band are independent in
+ * the same way (burners.rs:261-320 burns scanline by scanline).  Other
+ * arguments as rz_rasterize; a window outside the raster gives
+ * RZ_INVALID_ARGUMENT. */
+rz_status rz_rasterize_rows(rz_context* ctx, const rz_geoms* g, const void* values, const void* background,
+                            const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
+                            uint64_t row_begin, uint64_t row_end, rz_pixel_fn fn, rz_dtype out_dtype,
+                            uint32_t flags, void* out, rz_stats* stats, char* err, size_t errlen);
+
 /* ---- sparse (COO) encoding ------------------------------------------- */
 
 typedef struct rz_sparse rz_sparse;

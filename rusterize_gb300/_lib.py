@@ -127,6 +127,9 @@ PROTOTYPES = {
     "rz_rasterize": (c_int, [c_void_p, POINTER(RzGeoms), c_void_p, c_void_p, c_void_p, c_uint32,
                              POINTER(RzRasterInfo), c_int, c_int, c_uint32, c_void_p, POINTER(RzStats),
                              c_char_p, c_size_t]),
+    "rz_rasterize_rows": (c_int, [c_void_p, POINTER(RzGeoms), c_void_p, c_void_p, c_void_p, c_uint32,
+                                  POINTER(RzRasterInfo), c_uint64, c_uint64, c_int, c_int, c_uint32, c_void_p,
+                                  POINTER(RzStats), c_char_p, c_size_t]),
     "rz_rasterize_noalloc": (c_int, [c_void_p, POINTER(RzGeoms), c_void_p, c_void_p, c_void_p, c_uint32,
                                      POINTER(RzRasterInfo), c_int, c_int, c_uint32, c_void_p, POINTER(RzStats),
                                      c_char_p, c_size_t]),

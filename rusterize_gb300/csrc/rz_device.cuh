@@ -97,14 +97,20 @@ struct Grid {
 
 // The raster a part burns into, per job of a call (one entry for a single
 // call): its size, where its record words start, and the record flags of its
-// line and polygon parts.
+// line and polygon parts.  A call may burn only a window of its raster: the
+// rows [row_lo, row_hi) of the bands [band_lo, band_hi).  Every pixel
+// decision is still taken on the whole raster's grid (clipping, line
+// filters, walks), and only writes inside the window are kept, so the window
+// equals the same slice of a whole burn.
 struct JobDims {
   int nrows, ncols;
   unsigned ntx;        // 512-pixel column tiles per row
-  unsigned wid_base;   // first record word id of the job's raster
+  unsigned wid_base;   // first record word id of the job's window
   unsigned line_flag;  // DEDUP_BIT: line parts write each pixel once (PixelCache)
   unsigned poly_flag;  // DEDUP_BIT: polygon parts write each pixel once (all_touched sum / count)
   unsigned long long geom0;  // first geometry of the job
+  int row_lo, row_hi;        // window rows (whole raster: 0, nrows)
+  unsigned band_lo, band_hi; // window bands (whole raster: 0, bands)
 };
 
 struct Geo {
@@ -126,9 +132,11 @@ struct PartPlan {
   int wr;          // rows per window
   unsigned band;   // output band of the part
   int nrows, ncols;  // the part's raster
-  unsigned wid0;     // record word id of (band, row 0) in the part's raster
+  unsigned wid0;     // record word id of (band, row 0) of the part's raster, modulo 2^32
+                     // (a window that starts at row r puts row r at wid0 + r * wpr)
   unsigned wpr;      // record words per raster row (ntx * WPT)
   unsigned flags;    // flags of the part's records (DEDUP_BIT)
+  int rlo, rhi;      // rows of the window: pixels outside are not written
   unsigned pad;
 };
 

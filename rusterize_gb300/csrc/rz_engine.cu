@@ -100,14 +100,22 @@ fill_fn fill_for(rz_dtype dt) {
   return nullptr;
 }
 
-// the scatter, instantiated for the value size of the output dtype
-void launch_scatter(size_t tsize, int sms, cudaStream_t s, const RecBuf& sb, const unsigned* boff, unsigned* bcount,
-                    uint2* sorted, const void* values, const unsigned* part_geom, void* rvals, Ctrl* ctrl) {
+void launch_scatter(int sms, cudaStream_t s, const RecBuf& sb, const unsigned* boff, unsigned* bcount, uint2* sorted,
+                    Ctrl* ctrl) {
+  k_scatter<<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, ctrl);
+}
+
+// The burn value of every part (values[part_geom[p]], tsize bytes each).
+void launch_part_values(size_t tsize, int sms, cudaStream_t s, const unsigned* part_geom, const void* values,
+                        unsigned long long n_parts, void* pvals, Ctrl* ctrl) {
+  if (!n_parts) return;
+  const unsigned long long g0 = (n_parts + 255) / 256;
+  const unsigned grid = (unsigned)std::min<unsigned long long>(g0, (unsigned long long)sms * 16);
   switch (tsize) {
-    case 1: k_scatter<1><<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, values, part_geom, rvals, ctrl); break;
-    case 2: k_scatter<2><<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, values, part_geom, rvals, ctrl); break;
-    case 4: k_scatter<4><<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, values, part_geom, rvals, ctrl); break;
-    default: k_scatter<8><<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, values, part_geom, rvals, ctrl); break;
+    case 1: k_part_values<1><<<grid, 256, 0, s>>>(part_geom, values, n_parts, pvals, ctrl); break;
+    case 2: k_part_values<2><<<grid, 256, 0, s>>>(part_geom, values, n_parts, pvals, ctrl); break;
+    case 4: k_part_values<4><<<grid, 256, 0, s>>>(part_geom, values, n_parts, pvals, ctrl); break;
+    default: k_part_values<8><<<grid, 256, 0, s>>>(part_geom, values, n_parts, pvals, ctrl); break;
   }
 }
 
@@ -183,6 +191,10 @@ JobDims job_dims(unsigned long long nrows, unsigned long long ncols, const rz_ra
   jd.line_flag = (dedup || (sparse && line_dedup)) ? DEDUP_BIT : 0u;
   jd.poly_flag = touched && dedup ? DEDUP_BIT : 0u;
   jd.geom0 = geom0;
+  jd.row_lo = 0;  // the whole raster
+  jd.row_hi = (int)nrows;
+  jd.band_lo = 0;
+  jd.band_hi = 0xFFFFFFFFu;
   return jd;
 }
 
@@ -270,7 +282,7 @@ struct rz_context {
   int narrow_blocks_per_sm = 1;
   cudaStream_t stream = nullptr;
   DevBuf main, spans, out, sparse, batch, stage;
-  cudaEvent_t ev[8] = {};
+  cudaEvent_t ev[9] = {};
   Ctrl* h_ctrl = nullptr;  // pinned
   unsigned long long span_cap_hint = 0;
   unsigned char* h_stage = nullptr;  // pinned staging of batch tables and host job inputs
@@ -311,7 +323,7 @@ extern "C" rz_status rz_context_create(int device, rz_context** out, char* err, 
   cudaError_t e2 = cudaSetDevice(device);
   if (e2 == cudaSuccess) e2 = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e2 == cudaSuccess) e2 = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-  for (int i = 0; i < 8 && e2 == cudaSuccess; ++i) e2 = cudaEventCreate(&ctx->ev[i]);
+  for (int i = 0; i < 9 && e2 == cudaSuccess; ++i) e2 = cudaEventCreate(&ctx->ev[i]);
   if (e2 == cudaSuccess) e2 = cudaMallocHost((void**)&ctx->h_ctrl, sizeof(Ctrl));
   if (e2 == cudaSuccess)
     e2 = cudaFuncSetAttribute(k_poly_spans, cudaFuncAttributeMaxDynamicSharedMemorySize, POLY_SMEM);
@@ -397,13 +409,22 @@ static rz_status drain_on_error(cudaStream_t s, rz_status st) {
   return st;
 }
 
+// One pass of a burn: the bands [b0, b1) and rows [r0, r1) of the raster.
+struct PassWin {
+  unsigned long long b0, b1, r0, r1;
+};
+
 // The burn pipeline shared by the dense and the sparse entry points; with
 // `sp` the coverage records are turned into COO triplets instead of being
-// scattered into buckets and filled.
+// scattered into buckets and filled.  Only rows [row_lo, row_hi) of the
+// raster are burned (every band), into an output of that many rows per band.
+// The geometry is uploaded once; the window is then burned in passes of fewer
+// than 2^28 (band, row, tile) buckets each (one pass unless the raster is
+// very large), every pass into its own slab of the output.
 static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* values, const void* background,
                            const uint32_t* band_of_geom, uint32_t n_bands, const rz_raster_info* info,
-                           rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats, char* err,
-                           size_t errlen, rz_sparse* sp) {
+                           uint64_t row_lo, uint64_t row_hi, rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out,
+                           rz_stats* stats, char* err, size_t errlen, rz_sparse* sp) {
   using clk = std::chrono::steady_clock;
   const auto t_host0 = clk::now();
   rz::clear_err(err, errlen);
@@ -420,11 +441,29 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   if (info->nrows >= (1ull << 31) - 1 || info->ncols >= (1ull << 31) - 1)
     return fail(err, errlen, RZ_VALUE_ERROR, "raster dimensions must be below 2^31-1");
   const unsigned long long nrows = info->nrows, ncols = info->ncols;
-  const unsigned long long out_elems = nb * nrows * ncols;
+  if (row_lo > row_hi || row_hi > nrows)
+    return fail(err, errlen, RZ_INVALID_ARGUMENT, "row window [%llu, %llu) is outside the raster's %llu rows",
+                (unsigned long long)row_lo, (unsigned long long)row_hi, nrows);
+  const unsigned long long wrows = row_hi - row_lo;
+  const unsigned long long out_elems = nb * wrows * ncols;
   const unsigned ntx = (unsigned)((ncols + TW - 1) >> TW_SHIFT);
-  const unsigned long long nbuckets = nb * nrows * ntx;
-  if (nbuckets >= (1ull << 28))
-    return fail(err, errlen, RZ_VALUE_ERROR, "raster too large: more than 2^28 (band,row,tile) buckets");
+  // passes of fewer than 2^28 buckets: the whole window, or one band and a
+  // run of its rows at a time
+  constexpr unsigned long long kMaxBuckets = (1ull << 28) - 1;
+  std::vector<PassWin> passes;
+  if (nb * wrows * ntx <= kMaxBuckets) {
+    passes.push_back({0, nb, row_lo, row_hi});
+  } else {
+    if (sp) return fail(err, errlen, RZ_VALUE_ERROR, "raster too large: more than 2^28 (band,row,tile) buckets");
+    const unsigned long long rc = std::max<unsigned long long>(1, kMaxBuckets / std::max(1u, ntx));
+    for (unsigned long long b = 0; b < nb; ++b)
+      for (unsigned long long r0 = row_lo; r0 < row_hi; r0 += rc) passes.push_back({b, b + 1, r0, std::min(r0 + rc, (unsigned long long)row_hi)});
+  }
+  unsigned long long max_buckets = 0, pass_elems = 0;  // the largest pass
+  for (const PassWin& w : passes) {
+    max_buckets = std::max(max_buckets, (w.b1 - w.b0) * (w.r1 - w.r0) * ntx);
+    pass_elems = std::max(pass_elems, (w.b1 - w.b0) * (w.r1 - w.r0) * ncols);
+  }
   const unsigned long long G = g->n_geoms, P = g->n_parts, R = g->n_rings, V = g->n_vertices;
   if (G >= 0xFFFFFFFFull || P >= (1ull << 27))
     return fail(err, errlen, RZ_VALUE_ERROR, "at most 2^32-1 geometries and 2^27 parts are supported");
@@ -468,6 +507,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     if (band_of_geom) o_band = L.take(4 * (G ? G : 1));
   }
   const size_t o_pg = L.take(4 * (P ? P : 1));
+  const size_t o_pval = L.take(tsize * (P ? P : 1));
   const size_t o_plan = L.take(sizeof(PartPlan) * (P ? P : 1));
   const size_t o_cnt = L.take(8 * PC_N * (P ? P : 1));
   const size_t o_poff = L.take(8 * PC_N * (P + 1));
@@ -475,13 +515,13 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   const size_t o_last = L.take(8 * (P ? P : 1));
   const size_t o_lp = L.take(4 * (P ? P : 1));
   const size_t o_pp = L.take(4 * (P ? P : 1));
-  const size_t o_bc = L.take(4 * nbuckets);
-  const size_t o_boff = L.take(4 * (nbuckets + 1));
-  const size_t o_tmp32 = L.take(4 * scan_temp_elems(nbuckets, 1));
-  const size_t o_big = L.take(4 * nbuckets);
+  const size_t o_bc = L.take(4 * max_buckets);
+  const size_t o_boff = L.take(4 * (max_buckets + 1));
+  const size_t o_tmp32 = L.take(4 * scan_temp_elems(max_buckets, 1));
+  const size_t o_big = L.take(4 * max_buckets);
   const size_t o_ctrl = L.take(sizeof(Ctrl));
   RZ_CUDA(ensure(ctx->main, L.off));
-  if (!out_dev && !sp) RZ_CUDA(ensure(ctx->out, out_elems * tsize));
+  if (!out_dev && !sp) RZ_CUDA(ensure(ctx->out, pass_elems * tsize));
   unsigned long long cap = rzl::record_cap_request(std::max<unsigned long long>(ctx->span_cap_hint, 2 * V + (1ull << 20)));
 
   char* mb = static_cast<char*>(ctx->main.p);
@@ -518,11 +558,10 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     geo.xy = reinterpret_cast<const double2*>(g->xy);
     geo.bands = band_of_geom;
   }
-  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[1], s));
+  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[8], s));
 
   const bool touched = (flags & RZ_FLAG_ALL_TOUCHED) != 0;
   const Grid gr = make_grid(info, touched);
-  const JobDims one = job_dims(nrows, ncols, info, fn, touched, sp != nullptr, 0u, 0ull);
   const bool dedup = fill_dedup(info, fn, touched);
 
   Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
@@ -536,221 +575,249 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   unsigned* bcount = static_cast<unsigned*>(at(o_bc));
   unsigned* boff = static_cast<unsigned*>(at(o_boff));
   unsigned* big = static_cast<unsigned*>(at(o_big));
-  void* d_out = out_dev ? out : ctx->out.p;
   const int sms = ctx->num_sms;
   int launches = 0;
-
-  // ---- prep ----
-  RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
-  PartTables pt;
-  pt.part_geom = part_geom;
-  pt.plan = plan;
-  pt.counts = counts;
-  pt.poff = poff;
-  pt.tmp64 = static_cast<unsigned long long*>(at(o_tmp64));
-  pt.line_parts = line_parts;
-  pt.point_parts = point_parts;
-  pt.last_kept = last_kept;
-  launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sms, s);
-  RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
-  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[2], s));
-
-  const fill_fn fill = fill_for(dt);
   unsigned reruns = 0;
-  while (true) {
-    RZ_CUDA(ensure(ctx->spans, rzl::record_bytes_for(cap)));
-    const rzl::RecordLayout RL = rzl::record_layout(ctx->spans.cap);  // the whole buffer: cap or more
-    cap = RL.cap;
-    if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[7], s));
-    char* rbase = static_cast<char*>(ctx->spans.p);
-    RecBuf sb;
-    sb.cap = cap;
-    sb.nbuckets = nbuckets;
-    sb.wid = reinterpret_cast<unsigned*>(rbase + RL.off_wid);
-    sb.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
-    sb.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
-    uint2* sorted = reinterpret_cast<uint2*>(rbase + RL.off_sorted);
-    void* rvals = rbase + RL.off_rvals;
-    k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
-    RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
-    launches += 1;
-    launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sms, ctx->narrow_blocks_per_sm,
-                                ctx->poly_blocks_per_sm, s);
-    if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[3], s));
-    if (!sp) {
-    launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
-    launch_scatter(tsize, sms, s, sb, boff, bcount, sorted, d_values, part_geom, rvals, d_ctrl);
-    ++launches;
-    if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
-    FillArgs fa;
-    fa.offsets = boff;
-    fa.recs = sorted;
-    fa.rvals = d_values ? rvals : nullptr;
-    fa.nbuckets = nbuckets;
-    fa.scalar = scalar_bits;
-    fa.out = d_out;
-    set_background(fa, bg_bits, tsize);
-    fa.nrows = (int)(nb * nrows);  // rows of the band stack
-    fa.ncols = (int)ncols;
-    fa.ntx = ntx;
-    fa.big = big;
-    fa.ctrl = d_ctrl;
-    fa.rec_cap = cap;
-    fa.work = &d_ctrl->fill_work;
-    fa.nbig = &d_ctrl->big_count;
-    fa.jobs = nullptr;
-    fa.n_jobs = 0;
-    fa.bucket0 = 0;
-    launches += fill(fa, (int)fn, dedup, sms, s);
+  const fill_fn fill = fill_for(dt);
+  float ms_acc[4] = {0.f, 0.f, 0.f, 0.f};  // prep, spans, bucket, fill over the passes
+  unsigned long long pass_buckets = 0;
+
+  for (const PassWin& pw : passes) {
+    const unsigned long long nbuckets = (pw.b1 - pw.b0) * (pw.r1 - pw.r0) * ntx;
+    pass_buckets += nbuckets;
+    // this pass's slab of the output: band b0, row r0 of the window
+    const size_t out_off = (size_t)((pw.b0 * wrows + (pw.r0 - row_lo)) * ncols * tsize);
+    void* d_out = out_dev ? static_cast<void*>(static_cast<char*>(out) + out_off) : ctx->out.p;
+    JobDims one = job_dims(nrows, ncols, info, fn, touched, sp != nullptr, 0u, 0ull);
+    one.row_lo = (int)pw.r0;
+    one.row_hi = (int)pw.r1;
+    one.band_lo = (unsigned)pw.b0;
+    one.band_hi = (unsigned)pw.b1;
+    if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[1], s));
+
+    // ---- prep ----
+    RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
+    PartTables pt;
+    pt.part_geom = part_geom;
+    pt.plan = plan;
+    pt.counts = counts;
+    pt.poff = poff;
+    pt.tmp64 = static_cast<unsigned long long*>(at(o_tmp64));
+    pt.line_parts = line_parts;
+    pt.point_parts = point_parts;
+    pt.last_kept = last_kept;
+    launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sms, s);
+    if (d_values && !sp && P) {
+      launch_part_values(tsize, sms, s, part_geom, d_values, P, at(o_pval), d_ctrl);
+      ++launches;
     }
-    RZ_CUDA(cudaGetLastError());
-    if (timing) {
-      if (sp) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
-      RZ_CUDA(cudaEventRecord(ctx->ev[5], s));
-    }
-    RZ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
-    RZ_CUDA(cudaStreamSynchronize(s));
-    const Ctrl& hc = *ctx->h_ctrl;
-    if (hc.err) return ctrl_error(hc, err, errlen);
-    if (hc.span_count > cap) {
-      cap = rzl::record_cap_regrow(hc.span_count);
-      if (cap == 0) return fail(err, errlen, RZ_VALUE_ERROR, "more than 2^32 coverage records in one call");
-      ++reruns;
-      continue;
-    }
-    ctx->span_cap_hint = std::max(ctx->span_cap_hint, cap);  // only once a pass fitted
-    if (stats) {
-      stats->edges = hc.edges;
-      stats->crossings = hc.crossings;
-      stats->spans = hc.span_count;
-      stats->pixel_writes = hc.pixel_writes;
-      stats->big_buckets = hc.big_count;
-    }
-    break;
-  }
-  if (sp) {
-    // ---- sparse: order the records by (band, part, row, word), expand ----
-    const unsigned long long n = ctx->h_ctrl->span_count;
-    const rzl::RecordLayout RL = rzl::record_layout(ctx->spans.cap);
-    char* rbase = static_cast<char*>(ctx->spans.p);
-    RecBuf sbr;
-    sbr.cap = cap;
-    sbr.nbuckets = nbuckets;
-    sbr.wid = reinterpret_cast<unsigned*>(rbase + RL.off_wid);
-    sbr.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
-    sbr.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
-    const unsigned long long nsort = std::max<unsigned long long>(n, nb > 1 ? P : 0);
-    Layout SL;
-    const size_t o_k0 = SL.take(8 * (nsort ? nsort : 1)), o_k1 = SL.take(8 * (nsort ? nsort : 1));
-    const size_t o_v0 = SL.take(4 * (nsort ? nsort : 1)), o_v1 = SL.take(4 * (nsort ? nsort : 1));
-    const size_t o_pr = SL.take(4 * (P ? P : 1));
-    const size_t o_eff = SL.take(4 * (n ? n : 1));
-    const size_t o_cnt2 = SL.take(8 * (n + 1));
-    const size_t o_off2 = SL.take(8 * (n + 1));
-    const size_t o_st64 = SL.take(8 * scan_temp_elems(n ? n : 1, 1));
-    const size_t o_rst = SL.take(4 * radix_sort_temp_words(nsort ? nsort : 1));
-    const size_t o_bc = SL.take(8 * nb);
-    const size_t base_bytes = SL.off;
-    RZ_CUDA(ensure(ctx->sparse, base_bytes));
-    char* sbase = static_cast<char*>(ctx->sparse.p);
-    auto sat = [&](size_t o) { return static_cast<void*>(sbase + o); };
-    unsigned long long* k0 = static_cast<unsigned long long*>(sat(o_k0));
-    unsigned long long* k1 = static_cast<unsigned long long*>(sat(o_k1));
-    unsigned* v0 = static_cast<unsigned*>(sat(o_v0));
-    unsigned* v1 = static_cast<unsigned*>(sat(o_v1));
-    unsigned* prank = nullptr;
-    int bits_part = 1;
-    while ((1ull << bits_part) < P) ++bits_part;
-    if (nb > 1 && P) {  // band-major rank of every part
-      k_part_band_keys<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(plan, P, k0, v0);
-      int bits_band = 1;
-      while ((1ull << bits_band) < nb) ++bits_band;
-      const bool in_tmp = radix_sort(k0, v0, k1, v1, (unsigned)P, 32 + bits_band,
-                                     static_cast<unsigned*>(sat(o_rst)), s, launches);
-      prank = static_cast<unsigned*>(sat(o_pr));
-      k_part_rank<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(in_tmp ? v1 : v0, P, prank);
-      launches += 2;
-    }
-    unsigned long long* skeys = k0;
-    unsigned* svals = v0;
-    unsigned long long total = 0;
-    unsigned long long* bcnt = static_cast<unsigned long long*>(sat(o_bc));
-    RZ_CUDA(cudaMemsetAsync(bcnt, 0, 8 * nb, s));
-    if (n) {
-      k_rec_keys<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(sbr, n, prank, plan, k0, v0);
-      const bool in_tmp = radix_sort(k0, v0, k1, v1, (unsigned)n, 32 + bits_part,
-                                     static_cast<unsigned*>(sat(o_rst)), s, launches);
-      skeys = in_tmp ? k1 : k0;
-      svals = in_tmp ? v1 : v0;
-      unsigned* eff = static_cast<unsigned*>(sat(o_eff));
-      unsigned long long* cnt = static_cast<unsigned long long*>(sat(o_cnt2));
-      unsigned long long* off = static_cast<unsigned long long*>(sat(o_off2));
-      k_sparse_count<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(skeys, svals, n, sbr, eff, cnt);
-      launches += 2 + scan<unsigned long long, 1>(cnt, off, n, static_cast<unsigned long long*>(sat(o_st64)), s);
-      RZ_CUDA(cudaMemcpyAsync(&total, off + n, 8, cudaMemcpyDeviceToHost, s));
-      RZ_CUDA(cudaStreamSynchronize(s));
-      sp->rows.resize(total);
-      sp->cols.resize(total);
-      sp->values.resize(total * tsize);
-      if (total) {
-        // the triplet arrays go after the sort scratch (grow-only buffer)
-        const size_t o_rows = (base_bytes + 255) & ~size_t(255);
-        const size_t o_cols = o_rows + ((8 * total + 255) & ~size_t(255));
-        const size_t o_vals = o_cols + ((8 * total + 255) & ~size_t(255));
-        const size_t need = o_vals + tsize * total;
-        if (need > ctx->sparse.cap) {
-          // keep the ordered records: copy the live part of the scratch
-          DevBuf grown;
-          RZ_CUDA(ensure(grown, need));
-          RZ_CUDA(cudaMemcpyAsync(grown.p, ctx->sparse.p, base_bytes, cudaMemcpyDeviceToDevice, s));
-          RZ_CUDA(cudaStreamSynchronize(s));
-          cudaFree(ctx->sparse.p);
-          ctx->sparse = grown;
-          sbase = static_cast<char*>(ctx->sparse.p);
-          skeys = static_cast<unsigned long long*>(sat(in_tmp ? o_k1 : o_k0));
-          svals = static_cast<unsigned*>(sat(in_tmp ? o_v1 : o_v0));
-          eff = static_cast<unsigned*>(sat(o_eff));
-          off = static_cast<unsigned long long*>(sat(o_off2));
-          bcnt = static_cast<unsigned long long*>(sat(o_bc));
-        }
-        unsigned long long* trows = static_cast<unsigned long long*>(sat(o_rows));
-        unsigned long long* tcols = static_cast<unsigned long long*>(sat(o_cols));
-        void* tvals = sat(o_vals);
-        const unsigned eg = grid_for(n, 256, sms * 16);
-        switch (tsize) {
-          case 1: k_sparse_emit<1><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
-                                                      scalar_bits, trows, tcols, tvals, bcnt); break;
-          case 2: k_sparse_emit<2><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
-                                                      scalar_bits, trows, tcols, tvals, bcnt); break;
-          case 4: k_sparse_emit<4><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
-                                                      scalar_bits, trows, tcols, tvals, bcnt); break;
-          default: k_sparse_emit<8><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values,
-                                                       part_geom, scalar_bits, trows, tcols, tvals, bcnt); break;
-        }
+    RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
+    if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[2], s));
+
+    while (true) {
+      RZ_CUDA(ensure(ctx->spans, rzl::record_bytes_for(cap)));
+      const rzl::RecordLayout RL = rzl::record_layout(ctx->spans.cap);  // the whole buffer: cap or more
+      cap = RL.cap;
+      if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[7], s));
+      char* rbase = static_cast<char*>(ctx->spans.p);
+      RecBuf sb;
+      sb.cap = cap;
+      sb.nbuckets = nbuckets;
+      sb.wid = reinterpret_cast<unsigned*>(rbase + RL.off_wid);
+      sb.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
+      sb.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
+      uint2* sorted = reinterpret_cast<uint2*>(rbase + RL.off_sorted);
+      k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
+      RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
+      launches += 1;
+      launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sms, ctx->narrow_blocks_per_sm,
+                                  ctx->poly_blocks_per_sm, s);
+      if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[3], s));
+      if (!sp) {
+        launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
+        launch_scatter(sms, s, sb, boff, bcount, sorted, d_ctrl);
         ++launches;
-        RZ_CUDA(cudaGetLastError());
-        RZ_CUDA(cudaMemcpyAsync(sp->rows.data(), trows, 8 * total, cudaMemcpyDeviceToHost, s));
-        RZ_CUDA(cudaMemcpyAsync(sp->cols.data(), tcols, 8 * total, cudaMemcpyDeviceToHost, s));
-        RZ_CUDA(cudaMemcpyAsync(sp->values.data(), tvals, tsize * total, cudaMemcpyDeviceToHost, s));
+        if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
+        FillArgs fa;
+        fa.offsets = boff;
+        fa.recs = sorted;
+        fa.pvals = d_values ? at(o_pval) : nullptr;
+        fa.nbuckets = nbuckets;
+        fa.scalar = scalar_bits;
+        fa.out = d_out;
+        set_background(fa, bg_bits, tsize);
+        fa.nrows = (int)((pw.b1 - pw.b0) * (pw.r1 - pw.r0));  // rows of the pass's band stack
+        fa.ncols = (int)ncols;
+        fa.ntx = ntx;
+        fa.big = big;
+        fa.ctrl = d_ctrl;
+        fa.rec_cap = cap;
+        fa.work = &d_ctrl->fill_work;
+        fa.nbig = &d_ctrl->big_count;
+        fa.jobs = nullptr;
+        fa.n_jobs = 0;
+        fa.bucket0 = 0;
+        launches += fill(fa, (int)fn, dedup, sms, s);
       }
+      RZ_CUDA(cudaGetLastError());
+      if (timing) {
+        if (sp) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
+        RZ_CUDA(cudaEventRecord(ctx->ev[5], s));
+      }
+      RZ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+      RZ_CUDA(cudaStreamSynchronize(s));
+      const Ctrl& hc = *ctx->h_ctrl;
+      if (hc.err) return ctrl_error(hc, err, errlen);
+      if (hc.span_count > cap) {
+        cap = rzl::record_cap_regrow(hc.span_count);
+        if (cap == 0) return fail(err, errlen, RZ_VALUE_ERROR, "more than 2^32 coverage records in one call");
+        ++reruns;
+        continue;
+      }
+      ctx->span_cap_hint = std::max(ctx->span_cap_hint, cap);  // only once a pass fitted
+      if (stats) {
+        stats->edges += hc.edges;
+        stats->crossings += hc.crossings;
+        stats->spans += hc.span_count;
+        stats->pixel_writes += hc.pixel_writes;
+        stats->big_buckets += hc.big_count;
+      }
+      if (timing) {
+        float t[4] = {0.f, 0.f, 0.f, 0.f};
+        cudaEventElapsedTime(&t[0], ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&t[1], ctx->ev[7], ctx->ev[3]);
+        cudaEventElapsedTime(&t[2], ctx->ev[3], ctx->ev[4]);
+        cudaEventElapsedTime(&t[3], ctx->ev[4], ctx->ev[5]);
+        for (int k = 0; k < 4; ++k) ms_acc[k] += t[k];
+      }
+      break;
     }
-    RZ_CUDA(cudaMemcpyAsync(sp->band_counts.data(), bcnt, 8 * nb, cudaMemcpyDeviceToHost, s));
-    if (stats) stats->pixel_writes = total;
-  } else if (!out_dev) {
-    RZ_CUDA(cudaMemcpyAsync(out, d_out, out_elems * tsize, cudaMemcpyDeviceToHost, s));
-  }
-  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[6], s));
+    if (sp) {
+      // ---- sparse: order the records by (band, part, row, word), expand ----
+      const unsigned long long n = ctx->h_ctrl->span_count;
+      const rzl::RecordLayout RL = rzl::record_layout(ctx->spans.cap);
+      char* rbase = static_cast<char*>(ctx->spans.p);
+      RecBuf sbr;
+      sbr.cap = cap;
+      sbr.nbuckets = nbuckets;
+      sbr.wid = reinterpret_cast<unsigned*>(rbase + RL.off_wid);
+      sbr.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
+      sbr.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
+      const unsigned long long nsort = std::max<unsigned long long>(n, nb > 1 ? P : 0);
+      Layout SL;
+      const size_t o_k0 = SL.take(8 * (nsort ? nsort : 1)), o_k1 = SL.take(8 * (nsort ? nsort : 1));
+      const size_t o_v0 = SL.take(4 * (nsort ? nsort : 1)), o_v1 = SL.take(4 * (nsort ? nsort : 1));
+      const size_t o_pr = SL.take(4 * (P ? P : 1));
+      const size_t o_eff = SL.take(4 * (n ? n : 1));
+      const size_t o_cnt2 = SL.take(8 * (n + 1));
+      const size_t o_off2 = SL.take(8 * (n + 1));
+      const size_t o_st64 = SL.take(8 * scan_temp_elems(n ? n : 1, 1));
+      const size_t o_rst = SL.take(4 * radix_sort_temp_words(nsort ? nsort : 1));
+      const size_t o_bc = SL.take(8 * nb);
+      const size_t base_bytes = SL.off;
+      RZ_CUDA(ensure(ctx->sparse, base_bytes));
+      char* sbase = static_cast<char*>(ctx->sparse.p);
+      auto sat = [&](size_t o) { return static_cast<void*>(sbase + o); };
+      unsigned long long* k0 = static_cast<unsigned long long*>(sat(o_k0));
+      unsigned long long* k1 = static_cast<unsigned long long*>(sat(o_k1));
+      unsigned* v0 = static_cast<unsigned*>(sat(o_v0));
+      unsigned* v1 = static_cast<unsigned*>(sat(o_v1));
+      unsigned* prank = nullptr;
+      int bits_part = 1;
+      while ((1ull << bits_part) < P) ++bits_part;
+      if (nb > 1 && P) {  // band-major rank of every part
+        k_part_band_keys<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(plan, P, k0, v0);
+        int bits_band = 1;
+        while ((1ull << bits_band) < nb) ++bits_band;
+        const bool in_tmp = radix_sort(k0, v0, k1, v1, (unsigned)P, 32 + bits_band,
+                                       static_cast<unsigned*>(sat(o_rst)), s, launches);
+        prank = static_cast<unsigned*>(sat(o_pr));
+        k_part_rank<<<grid_for(P, 256, sms * 16), 256, 0, s>>>(in_tmp ? v1 : v0, P, prank);
+        launches += 2;
+      }
+      unsigned long long* skeys = k0;
+      unsigned* svals = v0;
+      unsigned long long total = 0;
+      unsigned long long* bcnt = static_cast<unsigned long long*>(sat(o_bc));
+      RZ_CUDA(cudaMemsetAsync(bcnt, 0, 8 * nb, s));
+      if (n) {
+        k_rec_keys<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(sbr, n, prank, plan, k0, v0);
+        const bool in_tmp = radix_sort(k0, v0, k1, v1, (unsigned)n, 32 + bits_part,
+                                       static_cast<unsigned*>(sat(o_rst)), s, launches);
+        skeys = in_tmp ? k1 : k0;
+        svals = in_tmp ? v1 : v0;
+        unsigned* eff = static_cast<unsigned*>(sat(o_eff));
+        unsigned long long* cnt = static_cast<unsigned long long*>(sat(o_cnt2));
+        unsigned long long* off = static_cast<unsigned long long*>(sat(o_off2));
+        k_sparse_count<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(skeys, svals, n, sbr, eff, cnt);
+        launches += 2 + scan<unsigned long long, 1>(cnt, off, n, static_cast<unsigned long long*>(sat(o_st64)), s);
+        RZ_CUDA(cudaMemcpyAsync(&total, off + n, 8, cudaMemcpyDeviceToHost, s));
+        RZ_CUDA(cudaStreamSynchronize(s));
+        sp->rows.resize(total);
+        sp->cols.resize(total);
+        sp->values.resize(total * tsize);
+        if (total) {
+          // the triplet arrays go after the sort scratch (grow-only buffer)
+          const size_t o_rows = (base_bytes + 255) & ~size_t(255);
+          const size_t o_cols = o_rows + ((8 * total + 255) & ~size_t(255));
+          const size_t o_vals = o_cols + ((8 * total + 255) & ~size_t(255));
+          const size_t need = o_vals + tsize * total;
+          if (need > ctx->sparse.cap) {
+            // keep the ordered records: copy the live part of the scratch
+            DevBuf grown;
+            RZ_CUDA(ensure(grown, need));
+            RZ_CUDA(cudaMemcpyAsync(grown.p, ctx->sparse.p, base_bytes, cudaMemcpyDeviceToDevice, s));
+            RZ_CUDA(cudaStreamSynchronize(s));
+            cudaFree(ctx->sparse.p);
+            ctx->sparse = grown;
+            sbase = static_cast<char*>(ctx->sparse.p);
+            skeys = static_cast<unsigned long long*>(sat(in_tmp ? o_k1 : o_k0));
+            svals = static_cast<unsigned*>(sat(in_tmp ? o_v1 : o_v0));
+            eff = static_cast<unsigned*>(sat(o_eff));
+            off = static_cast<unsigned long long*>(sat(o_off2));
+            bcnt = static_cast<unsigned long long*>(sat(o_bc));
+          }
+          unsigned long long* trows = static_cast<unsigned long long*>(sat(o_rows));
+          unsigned long long* tcols = static_cast<unsigned long long*>(sat(o_cols));
+          void* tvals = sat(o_vals);
+          const unsigned eg = grid_for(n, 256, sms * 16);
+          switch (tsize) {
+            case 1: k_sparse_emit<1><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
+                                                        scalar_bits, trows, tcols, tvals, bcnt); break;
+            case 2: k_sparse_emit<2><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
+                                                        scalar_bits, trows, tcols, tvals, bcnt); break;
+            case 4: k_sparse_emit<4><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values, part_geom,
+                                                        scalar_bits, trows, tcols, tvals, bcnt); break;
+            default: k_sparse_emit<8><<<eg, 256, 0, s>>>(skeys, svals, n, sbr, eff, off, plan, d_values,
+                                                         part_geom, scalar_bits, trows, tcols, tvals, bcnt); break;
+          }
+          ++launches;
+          RZ_CUDA(cudaGetLastError());
+          RZ_CUDA(cudaMemcpyAsync(sp->rows.data(), trows, 8 * total, cudaMemcpyDeviceToHost, s));
+          RZ_CUDA(cudaMemcpyAsync(sp->cols.data(), tcols, 8 * total, cudaMemcpyDeviceToHost, s));
+          RZ_CUDA(cudaMemcpyAsync(sp->values.data(), tvals, tsize * total, cudaMemcpyDeviceToHost, s));
+        }
+      }
+      RZ_CUDA(cudaMemcpyAsync(sp->band_counts.data(), bcnt, 8 * nb, cudaMemcpyDeviceToHost, s));
+      if (stats) stats->pixel_writes = total;
+    } else if (!out_dev) {
+      const size_t bytes = (size_t)((pw.b1 - pw.b0) * (pw.r1 - pw.r0) * ncols * tsize);
+      RZ_CUDA(cudaMemcpyAsync(static_cast<char*>(out) + out_off, d_out, bytes, cudaMemcpyDeviceToHost, s));
+    }
+    if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[6], s));
+    if (passes.size() > 1) RZ_CUDA(cudaStreamSynchronize(s));  // the next pass reuses the output scratch
+  }  // passes
   RZ_CUDA(cudaStreamSynchronize(s));
   if (stats) {
-    stats->buckets = nbuckets;
+    stats->buckets = pass_buckets;
     stats->reruns = reruns;
     stats->kernel_launches = (uint32_t)launches;
     if (timing) {
-      cudaEventElapsedTime(&stats->ms_h2d, ctx->ev[0], ctx->ev[1]);
-      cudaEventElapsedTime(&stats->ms_prep, ctx->ev[1], ctx->ev[2]);
-      cudaEventElapsedTime(&stats->ms_spans, ctx->ev[7], ctx->ev[3]);
-      cudaEventElapsedTime(&stats->ms_bucket, ctx->ev[3], ctx->ev[4]);
-      cudaEventElapsedTime(&stats->ms_fill, ctx->ev[4], ctx->ev[5]);
+      cudaEventElapsedTime(&stats->ms_h2d, ctx->ev[0], ctx->ev[8]);
+      stats->ms_prep = ms_acc[0];
+      stats->ms_spans = ms_acc[1];
+      stats->ms_bucket = ms_acc[2];
+      stats->ms_fill = ms_acc[3];
       cudaEventElapsedTime(&stats->ms_d2h, ctx->ev[5], ctx->ev[6]);
       cudaEventElapsedTime(&stats->ms_device_total, ctx->ev[0], ctx->ev[6]);
     }
@@ -765,8 +832,18 @@ extern "C" rz_status rz_rasterize(rz_context* ctx, const rz_geoms* g, const void
                                   rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats,
                                   char* err, size_t errlen) {
   return drain_on_error(ctx ? ctx->stream : nullptr,
-                        burn_impl(ctx, g, values, background, band_of_geom, n_bands, info, fn, dt, flags, out, stats,
-                                  err, errlen, nullptr));
+                        burn_impl(ctx, g, values, background, band_of_geom, n_bands, info, 0, info ? info->nrows : 0,
+                                  fn, dt, flags, out, stats, err, errlen, nullptr));
+}
+
+extern "C" rz_status rz_rasterize_rows(rz_context* ctx, const rz_geoms* g, const void* values,
+                                       const void* background, const uint32_t* band_of_geom, uint32_t n_bands,
+                                       const rz_raster_info* info, uint64_t row_begin, uint64_t row_end,
+                                       rz_pixel_fn fn, rz_dtype dt, uint32_t flags, void* out, rz_stats* stats,
+                                       char* err, size_t errlen) {
+  return drain_on_error(ctx ? ctx->stream : nullptr,
+                        burn_impl(ctx, g, values, background, band_of_geom, n_bands, info, row_begin, row_end, fn,
+                                  dt, flags, out, stats, err, errlen, nullptr));
 }
 
 extern "C" rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, const void* values,
@@ -780,8 +857,9 @@ extern "C" rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, con
     return fail(err, errlen, RZ_INVALID_ARGUMENT, "the sparse encoding returns host arrays");
   auto* sp = new rz_sparse();
   const rz_status st = drain_on_error(ctx ? ctx->stream : nullptr,
-                                      burn_impl(ctx, g, values, nullptr, band_of_geom, n_bands, info, fn, dt, flags,
-                                                nullptr, stats, err, errlen, sp));
+                                      burn_impl(ctx, g, values, nullptr, band_of_geom, n_bands, info, 0,
+                                                info ? info->nrows : 0, fn, dt, flags, nullptr, stats, err, errlen,
+                                                sp));
   if (st != RZ_OK) {
     delete sp;
     return st;
@@ -885,6 +963,7 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   // scratch layout inside the static array (inputs and output are the caller's)
   Layout L;
   const size_t o_pg = L.take(4 * (P ? P : 1));
+  const size_t o_pval = L.take(tsize * (P ? P : 1));
   const size_t o_plan = L.take(sizeof(PartPlan) * (P ? P : 1));
   const size_t o_cnt = L.take(8 * PC_N * (P ? P : 1));
   const size_t o_poff = L.take(8 * PC_N * (P + 1));
@@ -988,6 +1067,11 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   pt.point_parts = point_parts;
   pt.last_kept = last_kept;
   launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sms, s);
+  const void* d_vals_na = per_geom_values ? values : nullptr;
+  if (d_vals_na && P) {
+    launch_part_values(tsize, sms, s, part_geom, d_vals_na, P, at(o_pval), d_ctrl);
+    ++launches;
+  }
   RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
   char* rbase = static_cast<char*>(at(o_spans));
   RecBuf sb;
@@ -997,19 +1081,17 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   sb.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
   sb.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
   uint2* sorted = reinterpret_cast<uint2*>(rbase + RL.off_sorted);
-  void* rvals = rbase + RL.off_rvals;
   k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
   RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
   ++launches;
   launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sms, nd.narrow_bps, nd.poly_bps, s);
   launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
-  const void* d_vals_na = per_geom_values ? values : nullptr;
-  launch_scatter(tsize, sms, s, sb, boff, bcount, sorted, d_vals_na, part_geom, rvals, d_ctrl);
+  launch_scatter(sms, s, sb, boff, bcount, sorted, d_ctrl);
   ++launches;
   FillArgs fa;
   fa.offsets = boff;
   fa.recs = sorted;
-  fa.rvals = d_vals_na ? rvals : nullptr;
+  fa.pvals = d_vals_na ? at(o_pval) : nullptr;
   fa.nbuckets = nbuckets;
   fa.scalar = scalar_bits;
   fa.out = out;
@@ -1156,6 +1238,7 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
   const size_t o_vo = L.take(8 * (Rt + 1)), o_xy = L.take(16 * (Vt ? Vt : 1)), o_val = L.take(tsize * (Gt ? Gt : 1));
   const size_t o_rc = L.take(Rt ? Rt : 1);
   const size_t o_pg = L.take(4 * (Pt ? Pt : 1));
+  const size_t o_pval = L.take(tsize * (Pt ? Pt : 1));
   const size_t o_plan = L.take(sizeof(PartPlan) * (Pt ? Pt : 1));
   const size_t o_cnt = L.take(8 * PC_N * (Pt ? Pt : 1));
   const size_t o_poff = L.take(8 * PC_N * (Pt + 1));
@@ -1305,6 +1388,10 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
   pt.point_parts = static_cast<unsigned*>(at(o_pp));
   pt.last_kept = static_cast<unsigned long long*>(at(o_last));
   launches += launch_prep(geo, ident, dims[0], d_dims, n, 0u, pt, d_ctrl, sms, s);
+  if (Pt) {  // every job's values are gathered per geometry into the wave table
+    launch_part_values(tsize, sms, s, pt.part_geom, w_val, Pt, at(o_pval), d_ctrl);
+    ++launches;
+  }
   RZ_CUDA(cudaMemsetAsync(pt.last_kept, 0, 8 * (Pt ? Pt : 1), s));
   unsigned* bcount = static_cast<unsigned*>(at(o_bc));
   unsigned* boff = static_cast<unsigned*>(at(o_boff));
@@ -1327,7 +1414,6 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
     sb.part = reinterpret_cast<unsigned*>(rbase + RL.off_part);
     sb.mask = reinterpret_cast<unsigned*>(rbase + RL.off_mask);
     uint2* sorted = reinterpret_cast<uint2*>(rbase + RL.off_sorted);
-    void* rvals = rbase + RL.off_rvals;
     k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
     RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * (nbuckets ? nbuckets : 1), s));
     RZ_CUDA(cudaMemsetAsync(gctr, 0, 16 * (n + 1), s));
@@ -1336,7 +1422,7 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
                                 ctx->poly_blocks_per_sm, s);
     if (nbuckets) {
       launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
-      launch_scatter(tsize, sms, s, sb, boff, bcount, sorted, w_val, pt.part_geom, rvals, d_ctrl);
+      launch_scatter(sms, s, sb, boff, bcount, sorted, d_ctrl);
       ++launches;
       // one fill per variant: a run of jobs with equal (fn, dedup, background)
       unsigned g = 0;
@@ -1350,7 +1436,7 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
           FillArgs fa;
           fa.offsets = boff + lo;
           fa.recs = sorted;
-          fa.rvals = rvals;
+          fa.pvals = at(o_pval);
           fa.nbuckets = hi - lo;
           fa.scalar = 0;
           fa.out = nullptr;
@@ -1477,7 +1563,7 @@ extern "C" rz_status rz_rasterize_batch(rz_context* ctx, const rz_job* jobs, siz
     // device footprint: rasters (host outputs), geometry, part tables, bucket
     // tables, and about 4 B of coverage records per raster pixel
     b.dev_bytes = (out_dev ? 0 : b.out_elems * tsize) + geo_bytes * (in_dev ? 1 : 2) +
-                  b.P * (4 + sizeof(PartPlan) + 16 * PC_N + 16) + 16 * b.buckets + 4 * b.out_elems;
+                  b.P * (4 + 8 + sizeof(PartPlan) + 16 * PC_N + 16) + 16 * b.buckets + 4 * b.out_elems;
     total_out += b.out_elems * tsize;
   }
   if (stats) {

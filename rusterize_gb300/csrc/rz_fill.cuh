@@ -26,9 +26,9 @@ struct FillJob {
 struct FillArgs {
   const unsigned* offsets;  // [nbuckets + 1]
   const uint2* recs;        // {part | word << REC_W_SHIFT | DEDUP_BIT, mask} grouped by bucket
-  const void* rvals;        // value of each record (T), or nullptr: every record burns `scalar`
+  const void* pvals;        // burn value of each part (T), or nullptr: every record burns `scalar`
   unsigned long long nbuckets;
-  unsigned long long scalar;  // raw bits of the single value when rvals == nullptr
+  unsigned long long scalar;  // raw bits of the single value when pvals == nullptr
   void* out;                // (bands, nrows, ncols)
   unsigned long long bg;    // raw bits of the background
   uint4 bg16;               // background replicated over 16 bytes
@@ -179,9 +179,11 @@ __device__ __forceinline__ T first_write(T v) {
   else return v;
 }
 
+// The burn value of a record: its part's value (values[geometry of the part],
+// gathered once per part by the prep), or the call's single value.
 template <typename T>
-__device__ __forceinline__ T rec_value(const FillArgs& a, unsigned long long idx) {
-  if (a.rvals) return static_cast<const T*>(a.rvals)[idx];
+__device__ __forceinline__ T rec_value(const FillArgs& a, unsigned rec_x) {
+  if (a.pvals) return static_cast<const T*>(a.pvals)[rec_x & REC_PART_MASK];
   return from_bits<T>(a.scalar);
 }
 
@@ -312,11 +314,11 @@ __device__ __forceinline__ LanePair<T> load_pair(const FillArgs& a, unsigned o0,
   if (n <= FILL_WARP_MAX) {
     if (lane < n) {
       p.r0 = a.recs[o0 + lane];
-      p.v0 = rec_value<T>(a, o0 + lane);
+      p.v0 = rec_value<T>(a, p.r0.x);
     }
     if (lane + 32 < n) {
       p.r1 = a.recs[o0 + lane + 32];
-      p.v1 = rec_value<T>(a, o0 + lane + 32);
+      p.v1 = rec_value<T>(a, p.r1.x);
     }
   }
   return p;
@@ -481,7 +483,7 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
           SRec e;
           e.key = r.x;
           e.mask = r.y;
-          e.vbits = to_bits<T>(rec_value<T>(a, o0 + i));
+          e.vbits = to_bits<T>(rec_value<T>(a, r.x));
           srec[i] = e;
           skey[i] = ((unsigned long long)(r.x & ~DEDUP_BIT) << 8) | (unsigned)i;
         }
@@ -712,7 +714,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
           // part (order), then the DEDUP flag, then the mask
           keys[pos] = ((unsigned long long)(r.x & REC_PART_MASK) << 33) | ((unsigned long long)(r.x >> 31) << 32) |
                       r.y;
-          vals[pos] = rec_value<T>(a, o0 + i);
+          vals[pos] = rec_value<T>(a, r.x);
         }
         m += __popc(mk);
         if (single && m > BIG_CAP - 32) {  // fold a chunk of the single part

@@ -88,9 +88,23 @@ __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restr
     pl.nrows = jd.nrows;
     pl.ncols = jd.ncols;
     pl.wpr = jd.ntx * WPT;
-    pl.wid0 = jd.wid_base + band * (unsigned)jd.nrows * pl.wpr;
+    // unsigned arithmetic wraps: row r of the window lands on wid0 + r * wpr
+    pl.wid0 = jd.wid_base + (band - jd.band_lo) * (unsigned)(jd.row_hi - jd.row_lo) * pl.wpr -
+              (unsigned)jd.row_lo * pl.wpr;
     pl.flags = kind == 1 ? jd.line_flag : (kind == 2 ? jd.poly_flag : 0u);
+    pl.rlo = jd.row_lo;
+    pl.rhi = jd.row_hi;
     pl.pad = 0;
+    // parts of bands outside the window burn nothing in this call
+    const bool in_window = band >= jd.band_lo && band < jd.band_hi && jd.row_lo < jd.row_hi;
+    if (!in_window) {
+      if (lane == 0) {
+        plan[p] = pl;
+#pragma unroll
+        for (int k = 0; k < PC_N; ++k) counts[p * PC_N + k] = 0;
+      }
+      continue;
+    }
     if (kind != 0) {
       // segments = vertices - non-empty rings
       unsigned long long nonempty = 0;
@@ -149,8 +163,8 @@ __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restr
       };
       if (ylo <= yhi) {
         // pixel y decreases with world y
-        const int row0 = row_ceil(to_py(g, unkey(yhi)), jd.nrows);
-        const int row1 = row_ceil(to_py(g, unkey(ylo)), jd.nrows);
+        const int row0 = max(row_ceil(to_py(g, unkey(yhi)), jd.nrows), jd.row_lo);
+        const int row1 = min(row_ceil(to_py(g, unkey(ylo)), jd.nrows), jd.row_hi);
         if (row1 > row0) {
           double c_lo = 0.0, c_hi = (double)jd.ncols;
           if (xlo <= xhi && !nan_x) {
@@ -199,10 +213,11 @@ __global__ void k_part_lists(Geo geo, const unsigned long long* off /*[P+1][PC_N
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < geo.n_parts;
        p += stride) {
-    const unsigned kind = geo.part_kind[p];
-    if (kind == 1 || (kind == 2 && off[(p + 1) * PC_N + PC_LINE_P] > off[p * PC_N + PC_LINE_P]))
+    // a part is listed when it was counted (parts outside the call's window are not)
+    if (off[(p + 1) * PC_N + PC_LINE_P] > off[p * PC_N + PC_LINE_P])
       line_parts[off[p * PC_N + PC_LINE_P]] = (unsigned)p;
-    else if (kind == 0) point_parts[off[p * PC_N + PC_POINT_P]] = (unsigned)p;
+    else if (off[(p + 1) * PC_N + PC_POINT_P] > off[p * PC_N + PC_POINT_P])
+      point_parts[off[p * PC_N + PC_POINT_P]] = (unsigned)p;
   }
 }
 
@@ -382,7 +397,7 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
       // polygon's PixelCache (sum / count only), not the non-square-pixel
       // cache of LineString::burn
       const bool ok = all_touched_walk(x0, y0, x1, y1, pl.nrows, pl.ncols, [&](int yy, int xx) {
-        run_add(run, sb, bucket_count, ctrl, pl, p, yy, xx);
+        if (yy >= pl.rlo && yy < pl.rhi) run_add(run, sb, bucket_count, ctrl, pl, p, yy, xx);
       });
       run_flush(run, sb, bucket_count, ctrl, pl, p);
       if (!ok) set_error(ctrl, ERR_LINE_LONG, v);
@@ -403,7 +418,7 @@ __global__ void k_line_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan,
     const long long sx = ix0 < ix1 ? 1 : -1, sy = iy0 < iy1 ? 1 : -1;
     long long err = dx + dy;
     while (ix0 != ix1 || iy0 != iy1) {
-      if (ix0 >= 0 && ix0 < pl.ncols && iy0 >= 0 && iy0 < pl.nrows)
+      if (ix0 >= 0 && ix0 < pl.ncols && iy0 >= pl.rlo && iy0 < pl.rhi)
         run_add(run, sb, bucket_count, ctrl, pl, p, (int)iy0, (int)ix0);
       const long long e2 = 2 * err;
       if (e2 >= dy) { err += dy; ix0 += sx; }
@@ -442,7 +457,7 @@ __global__ void k_line_endpix(Geo geo, Grid g, const PartPlan* __restrict__ plan
     const double2 w1 = geo.xy[v + 1];
     const long long ix = as_isize(floor(to_px(g, w1.x))), iy = as_isize(floor(to_py(g, w1.y)));
     const PartPlan pl = plan[p];
-    if (ix >= 0 && ix < pl.ncols && iy >= 0 && iy < pl.nrows) {
+    if (ix >= 0 && ix < pl.ncols && iy >= pl.rlo && iy < pl.rhi) {
       ++npix;
       emit_run(sb, bucket_count, ctrl, pl, (int)iy, (int)ix, (int)ix + 1, p | pl.flags);
     }
@@ -471,7 +486,8 @@ __global__ void k_point_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan
     const double2 w = geo.xy[v];
     const double x = to_px(g, w.x), y = to_py(g, w.y);
     const PartPlan pl = plan[p];
-    if (x >= 0.0 && x < (double)pl.ncols && y >= 0.0 && y < (double)pl.nrows) {
+    // extract_point keeps 0 <= y < nrows; the window keeps rows [rlo, rhi) of those
+    if (x >= 0.0 && x < (double)pl.ncols && y >= (double)pl.rlo && y < (double)pl.rhi) {
       ++npix;
       emit_run(sb, bucket_count, ctrl, pl, (int)y, (int)x, (int)x + 1, p);
     }
@@ -482,18 +498,12 @@ __global__ void k_point_spans(Geo geo, Grid g, const PartPlan* __restrict__ plan
 
 // ------------------------------------------------------------- scatter -----
 // Move each coverage record into its bucket's range as {part | word-in-tile
-// << REC_W_SHIFT | DEDUP_BIT, mask}, and its part's burn value (VB bytes,
-// values[part_geom[part]]) beside it, so the fill reads both with one
-// dependent load.  Order inside a bucket is arbitrary here; the fill kernels
-// restore part order.  Records of one bucket that sit in one warp
-// (neighbouring words of a row) take their slots with one atomic.
-template <int VB>
+// << REC_W_SHIFT | DEDUP_BIT, mask}.  Order inside a bucket is arbitrary
+// here; the fill kernels restore part order (and look up each part's burn
+// value).  Records of one bucket that sit in one warp (neighbouring words of
+// a row) take their slots with one atomic.
 __global__ void k_scatter(RecBuf sb, const unsigned* __restrict__ offsets, unsigned* counts, uint2* sorted,
-                          const void* __restrict__ values, const unsigned* __restrict__ part_geom, void* rvals,
                           Ctrl* ctrl) {
-  using V = typename std::conditional<VB == 1, unsigned char,
-            typename std::conditional<VB == 2, unsigned short,
-            typename std::conditional<VB == 4, unsigned, unsigned long long>::type>::type>::type;
   if (ctrl->err || ctrl->span_count > sb.cap) return;
   const unsigned long long n = ctrl->span_count;
   const int lane = threadIdx.x & 31;
@@ -510,13 +520,24 @@ __global__ void k_scatter(RecBuf sb, const unsigned* __restrict__ offsets, unsig
     if (valid && lane == leader) left = atomicSub(&counts[b], (unsigned)__popc(same));
     left = __shfl_sync(0xFFFFFFFFu, left, leader);
     if (valid) {
-      const unsigned part = sb.part[i];
       const unsigned rank = (unsigned)__popc(same & ((1u << lane) - 1u));
       const unsigned pos = offsets[b + 1] - left + rank;  // arrival order
-      sorted[pos] = make_uint2(part | ((wid % WPT) << REC_W_SHIFT), sb.mask[i]);
-      if (values) static_cast<V*>(rvals)[pos] = static_cast<const V*>(values)[part_geom[part & REC_PART_MASK]];
+      sorted[pos] = make_uint2(sb.part[i] | ((wid % WPT) << REC_W_SHIFT), sb.mask[i]);
     }
   }
+}
+
+// The burn value of every part (VB bytes): values[part_geom[p]].
+template <int VB>
+__global__ void k_part_values(const unsigned* __restrict__ part_geom, const void* __restrict__ values,
+                              unsigned long long n_parts, void* pvals, Ctrl* ctrl) {
+  using V = typename std::conditional<VB == 1, unsigned char,
+            typename std::conditional<VB == 2, unsigned short,
+            typename std::conditional<VB == 4, unsigned, unsigned long long>::type>::type>::type;
+  if (ctrl->err) return;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < n_parts; p += stride)
+    static_cast<V*>(pvals)[p] = static_cast<const V*>(values)[part_geom[p]];
 }
 
 }  // namespace rzd

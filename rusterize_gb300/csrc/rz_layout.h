@@ -3,15 +3,14 @@
 // arithmetic at its boundary sizes.
 //
 // One pass of span generation writes coverage records into one buffer cut
-// into five arrays of `cap` entries each:
+// into four arrays of `cap` entries each:
 //   wid[cap]     u32  word id of the record
 //   part[cap]    u32  part | flags
 //   mask[cap]    u32  covered pixels of the word
 //   sorted[cap]  u64  {part | word << 27 | flags, mask} grouped by bucket (uint2)
-//   rvals[cap]   <=8 B  burn value of each sorted record (1, 2, 4 or 8 bytes)
-// 28 bytes per record (RECORD_BYTES).  Record counts and bucket offsets are
+// 20 bytes per record (RECORD_BYTES).  Record counts and bucket offsets are
 // 32-bit on the device, so cap never exceeds RECORD_CAP_MAX, and cap is even
-// so that `sorted` and `rvals` start on 8-byte boundaries.
+// so that `sorted` starts on an 8-byte boundary.
 #pragma once
 
 #include <cstddef>
@@ -19,13 +18,13 @@
 
 namespace rzl {
 
-constexpr uint64_t RECORD_BYTES = 28;
+constexpr uint64_t RECORD_BYTES = 20;
 constexpr uint64_t RECORD_CAP_MAX = 0xFFFFFFF0ull;  // < 2^32: every record index and bucket offset fits in 32 bits
 constexpr uint64_t RECORD_PAD = 16;                 // slack after the last array
 
 struct RecordLayout {
   uint64_t cap = 0;  // records per array (even, <= RECORD_CAP_MAX)
-  uint64_t off_wid = 0, off_part = 0, off_mask = 0, off_sorted = 0, off_rvals = 0;
+  uint64_t off_wid = 0, off_part = 0, off_mask = 0, off_sorted = 0;
   uint64_t end = 0;  // bytes used (<= the buffer size)
 };
 
@@ -48,8 +47,7 @@ inline RecordLayout record_layout(uint64_t buffer_bytes) {
   L.off_part = 4 * L.cap;
   L.off_mask = 8 * L.cap;
   L.off_sorted = 12 * L.cap;  // cap even: a multiple of 8
-  L.off_rvals = 20 * L.cap;   // cap even: a multiple of 8
-  L.end = 28 * L.cap;
+  L.end = 20 * L.cap;
   return L;
 }
 

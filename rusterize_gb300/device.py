@@ -67,18 +67,20 @@ def upload(a: np.ndarray, device: int = 0):
 
 def rasterize_device(dt: DeviceTable, info: RasterInfo, *, fn: str, background, dtype: str, values=None,
                      bands=None, n_bands: int = 1, out=None, context: _lib.Context | None = None,
-                     stats: dict | None = None):
+                     stats: dict | None = None, rows: tuple[int, int] | None = None):
     """Burn a DeviceTable into a CUDA tensor (bands, nrows, ncols) of dtype.
     values: CUDA tensor of the output dtype's bits per geometry, or None (1);
-    bands: CUDA int32 tensor of band indices, or None."""
+    bands: CUDA int32 tensor of band indices, or None; rows: only the raster
+    rows [r0, r1), into (bands, r1 - r0, ncols) (``rz_rasterize_rows``)."""
     torch = _torch()
     lib = _lib.load()
     ctx = context or _lib.default_context()
     np_dt = np.dtype(dtype)
     tdt = {"uint8": torch.uint8, "int8": torch.int8, "int16": torch.int16, "int32": torch.int32,
            "int64": torch.int64, "float32": torch.float32, "float64": torch.float64}.get(dtype)
+    r0, r1 = (0, info.nrows) if rows is None else (int(rows[0]), int(rows[1]))
     if out is None:
-        shape = (n_bands, info.nrows, info.ncols)
+        shape = (n_bands, r1 - r0, info.ncols)
         if tdt is None:  # unsigned wider than 8 bits: raw bytes
             out = torch.empty(int(np.prod(shape)) * np_dt.itemsize, dtype=torch.uint8, device=dt.tensors["xy"].device)
         else:
@@ -92,9 +94,14 @@ def rasterize_device(dt: DeviceTable, info: RasterInfo, *, fn: str, background, 
     vals = values.data_ptr() if values is not None else None
     bptr = bands.data_ptr() if bands is not None else None
     with ctx.lock:
-        rc = lib.rz_rasterize(ctx.handle, ctypes.byref(g), vals, bg.ctypes.data, bptr, n_bands, ctypes.byref(ri),
-                              _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags, out.data_ptr(), ctypes.byref(st), e,
-                              len(e))
+        if rows is None:
+            rc = lib.rz_rasterize(ctx.handle, ctypes.byref(g), vals, bg.ctypes.data, bptr, n_bands,
+                                  ctypes.byref(ri), _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags, out.data_ptr(),
+                                  ctypes.byref(st), e, len(e))
+        else:
+            rc = lib.rz_rasterize_rows(ctx.handle, ctypes.byref(g), vals, bg.ctypes.data, bptr, n_bands,
+                                       ctypes.byref(ri), r0, r1, _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags,
+                                       out.data_ptr(), ctypes.byref(st), e, len(e))
     _lib.raise_for(rc, e.value)
     if stats is not None:
         stats.update(st.as_dict())

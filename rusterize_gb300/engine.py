@@ -75,12 +75,14 @@ def rasterize_table(table: GeometryTable, info: RasterInfo, *, values=None, fn: 
                     background=0, dtype: str = "float64", bands: np.ndarray | None = None,
                     n_bands: int | None = None, all_touched: bool = False,
                     context: _lib.Context | None = None, out: np.ndarray | None = None,
-                    stats: dict | None = None) -> np.ndarray:
+                    stats: dict | None = None, rows: tuple[int, int] | None = None) -> np.ndarray:
     """Burn ``table`` into a dense (bands, nrows, ncols) array of ``dtype``.
 
     values: None (burn 1), a scalar (FieldSource::Scalar) or a per-geometry
     array of ``dtype`` (FieldSource::Array).  bands: per-geometry band index
-    (uint32) with ``n_bands`` bands, or None for one band.
+    (uint32) with ``n_bands`` bands, or None for one band.  rows: burn only
+    the raster rows [r0, r1) (``rz_rasterize_rows``): the result is
+    (bands, r1 - r0, ncols) and equals those rows of the whole burn.
     """
     lib = _lib.load()
     if dtype not in _lib.DTYPES:
@@ -108,18 +110,27 @@ def rasterize_table(table: GeometryTable, info: RasterInfo, *, values=None, fn: 
                 raise ValueError("Geometry and field lengths must match")
         c_vals = vals_arr.ctypes.data
     bg = np.array([background], dtype=np_dt)
+    r0, r1 = (0, info.nrows) if rows is None else (int(rows[0]), int(rows[1]))
+    if not 0 <= r0 <= r1 <= info.nrows:
+        raise ValueError(f"rows {rows} are outside the raster's {info.nrows} rows")
+    shape = (nb, r1 - r0, info.ncols)
     if out is None:
-        out = np.empty((nb, info.nrows, info.ncols), dtype=np_dt)
-    elif out.dtype != np_dt or out.shape != (nb, info.nrows, info.ncols) or not out.flags.c_contiguous:
+        out = np.empty(shape, dtype=np_dt)
+    elif out.dtype != np_dt or out.shape != shape or not out.flags.c_contiguous:
         raise ValueError("out has the wrong dtype, shape or layout")
     g = table.c_view()
     ri = info.c_struct()
     st_c = _lib.RzStats()
     e = _lib.errbuf()
     with ctx.lock:
-        st = lib.rz_rasterize(ctx.handle, ctypes.byref(g), c_vals, bg.ctypes.data, c_bands, nb, ctypes.byref(ri),
-                              _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags, out.ctypes.data, ctypes.byref(st_c),
-                              e, len(e))
+        if rows is None:
+            st = lib.rz_rasterize(ctx.handle, ctypes.byref(g), c_vals, bg.ctypes.data, c_bands, nb,
+                                  ctypes.byref(ri), _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags, out.ctypes.data,
+                                  ctypes.byref(st_c), e, len(e))
+        else:
+            st = lib.rz_rasterize_rows(ctx.handle, ctypes.byref(g), c_vals, bg.ctypes.data, c_bands, nb,
+                                       ctypes.byref(ri), r0, r1, _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags,
+                                       out.ctypes.data, ctypes.byref(st_c), e, len(e))
     _lib.raise_for(st, e.value)
     if stats is not None:
         stats.update(st_c.as_dict())

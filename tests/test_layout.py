@@ -1,7 +1,7 @@
 """Host-side checks of the record-scratch sizing (rusterize_gb300/csrc/rz_layout.h)
 at its boundary sizes: the arrays of one pass never overlap, stay inside the
 buffer, start on the alignment of their element type (8 bytes for the
-sorted uint2 records and for 8-byte burn values), and every record index
+sorted uint2 records), and every record index
 and bucket offset fits in 32 bits.  The header is compiled with g++ into a
 small checker that prints one line per case."""
 
@@ -35,9 +35,8 @@ static void check_layout(uint64_t bytes) {
   CHECK(L.end + RECORD_PAD <= bytes || L.cap == 0, "no pad for %llu", (unsigned long long)bytes);
   // arrays in order, each cap elements long
   CHECK(L.off_part == L.off_wid + 4 * L.cap && L.off_mask == L.off_part + 4 * L.cap, "u32 arrays overlap");
-  CHECK(L.off_sorted == L.off_mask + 4 * L.cap && L.off_rvals == L.off_sorted + 8 * L.cap, "sorted overlaps");
-  CHECK(L.end == L.off_rvals + 8 * L.cap, "rvals size");
-  CHECK(L.off_sorted % 8 == 0 && L.off_rvals % 8 == 0, "alignment for %llu", (unsigned long long)bytes);
+  CHECK(L.off_sorted == L.off_mask + 4 * L.cap && L.end == L.off_sorted + 8 * L.cap, "sorted overlaps");
+  CHECK(L.off_sorted % 8 == 0, "alignment for %llu", (unsigned long long)bytes);
   // the largest record index and a bucket offset one past it fit in 32 bits
   CHECK(L.cap == 0 || L.cap - 1 <= 0xFFFFFFFFull, "index width");
   CHECK(L.cap <= 0xFFFFFFFFull, "offset width");
@@ -49,8 +48,9 @@ static void check_layout(uint64_t bytes) {
 
 int main() {
   const uint64_t base[] = {0, 1, 15, 16, 17, 28, 44, 71, 72, 73, 1000, 1ull << 20, 64ull << 20, 1ull << 32,
-                           28ull * 0xFFFFFFF0ull + 15, 28ull * 0xFFFFFFF0ull + 16, 28ull * 0xFFFFFFF0ull + 17,
-                           28ull * 0xFFFFFFF2ull + 16, 28ull * 0x100000000ull + 16, 1ull << 40, 1ull << 44};
+                           RECORD_BYTES * 0xFFFFFFF0ull + 15, RECORD_BYTES * 0xFFFFFFF0ull + 16,
+                           RECORD_BYTES * 0xFFFFFFF0ull + 17, RECORD_BYTES * 0xFFFFFFF2ull + 16,
+                           RECORD_BYTES * 0x100000000ull + 16, 1ull << 40, 1ull << 44};
   for (uint64_t b : base)
     for (int d = -40; d <= 40; ++d) {
       if ((int64_t)b + d < 0) continue;
