@@ -271,6 +271,19 @@ def run_gb300(args) -> None:
 
     for _ in range(args.warmup):
         step()
+    # the engine's schedule for this workload class, chosen by the autotuner
+    # (outside the timed region; results do not depend on it)
+    tuning = None
+    if args.tune:
+        from rusterize_gb300 import tune
+
+        def step_ms():
+            a, b = step()
+            return a["ms_device_total"] + b["ms_device_total"]
+
+        res = tune.autotune(ctx, step_ms, rounds=2, repeats=3, warmup=1)
+        tuning = dict(res.as_dict(), workload_class=tune.table_class(info.nrows, info.ncols, table.n_geoms,
+                                                                     table.n_vertices))
     acc: list = []
     barrier()
     torch.cuda.synchronize()
@@ -387,6 +400,7 @@ def run_gb300(args) -> None:
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": roofline,
+            "tuning": tuning,
             "cpu_baseline": cpu,
             "batched": batched,
             "served": served,
@@ -397,10 +411,12 @@ def run_gb300(args) -> None:
 
 
 def _batched_leg(args, ctx, local) -> dict:
-    """Uneven independent jobs (synth.batch_jobs: polygons per job lognormal
-    median 500, sides log-uniform 256-8192, f32, pixel functions drawn per
-    job), device-resident: the plain path (one rz_rasterize per job) against
-    the batched form (rz_rasterize_batch over all jobs), jobs/s and px/s."""
+    """Uneven independent jobs (synth.batch_jobs_fast: polygons per job
+    lognormal median 500, sides log-uniform 256-8192, f32, pixel functions
+    drawn per job; 4,096 jobs by default), device-resident: the plain path
+    (one rz_rasterize per job) against the batched form (rz_rasterize_batch
+    over all jobs), jobs/s and px/s, each with the schedule the autotuner
+    picks for it on a sample of the jobs."""
     import torch
 
     import rusterize_gb300 as rz
@@ -408,7 +424,7 @@ def _batched_leg(args, ctx, local) -> dict:
     from rusterize_gb300.device import DeviceTable, rasterize_batch_device, rasterize_device, upload
     from rusterize_gb300.engine import BatchJob
 
-    ws = synth.batch_jobs(seed=1004, n_jobs=args.batch_jobs)
+    ws = synth.batch_jobs_fast(seed=1004, n_jobs=args.batch_jobs)
     dev = torch.device("cuda", local)
     jobs, outs = [], []
     for w in ws:
@@ -441,9 +457,39 @@ def _batched_leg(args, ctx, local) -> dict:
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
+    # each leg runs with its own schedule, tuned on a sample of the jobs
+    from rusterize_gb300 import tune
+
+    ns = min(len(jobs), max(1, args.batch_tune_jobs))
+    sample_j, sample_o = jobs[:ns], outs[:ns]
+
+    def plain_sample_ms():
+        tot = 0.0
+        for j, o in zip(sample_j, sample_o):
+            st1: dict = {}
+            rasterize_device(j.table, j.info, fn=j.fn, background=j.background, dtype="float32", values=j.values,
+                             out=o, context=ctx, stats=st1)
+            tot += st1["ms_device_total"]
+        return tot
+
+    def batch_sample_ms():
+        st1: dict = {}
+        rasterize_batch_device(sample_j, dtype="float32", outs=sample_o, context=ctx, stats=st1)
+        return st1["ms_device_total"]
+
     legs = set(args.batch_legs.split(","))
-    ms_plain = timed(plain, args.batch_steps) if "plain" in legs else float("nan")
-    ms_batch = timed(batch, args.batch_steps) if "batched" in legs else float("nan")
+    tunings = {}
+    ms_plain = ms_batch = float("nan")
+    if "plain" in legs:
+        if args.tune:
+            tunings["plain"] = tune.autotune(ctx, plain_sample_ms, rounds=1, repeats=1, warmup=1).as_dict()
+        ms_plain = timed(plain, args.batch_steps)
+    if "batched" in legs:
+        if args.tune:
+            ctx.set_tuning(None)
+            tunings["batched"] = tune.autotune(ctx, batch_sample_ms, rounds=2, repeats=2, warmup=1).as_dict()
+        ms_batch = timed(batch, args.batch_steps)
+    ctx.set_tuning(None)
     n = len(jobs)
     out = {
         "workload": f"uneven_jobs_{n}_sides_256-8192_f32",
@@ -451,6 +497,10 @@ def _batched_leg(args, ctx, local) -> dict:
         "plain": {"ms": ms_plain, "jobs_per_s": n / (ms_plain / 1e3), "px_per_s": px / (ms_plain / 1e3)},
         "batched": {"ms": ms_batch, "jobs_per_s": n / (ms_batch / 1e3), "px_per_s": px / (ms_batch / 1e3),
                     "waves": st.get("waves"), "kernel_launches": st.get("kernel_launches")},
+        "batched_over_plain": ms_plain / ms_batch,
+        "tuning": dict(tunings, sample_jobs=ns,
+                       workload_class=tune.batch_class(n, px, sum(j.table.table.n_geoms for j in jobs),
+                                                       sum(j.table.table.n_vertices for j in jobs))),
         "note": "device-resident geometry and rasters; CUDA events on the engine stream; outputs larger than L2",
     }
     del jobs, outs
@@ -572,7 +622,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--batch-jobs", type=int, default=512, help="jobs of the batched leg (0: skip it)")
+    ap.add_argument("--batch-jobs", type=int, default=4096, help="jobs of the batched leg (0: skip it)")
+    ap.add_argument("--batch-tune-jobs", type=int, default=256, help="jobs of the sample each batched leg is tuned on")
+    ap.add_argument("--no-tune", dest="tune", action="store_false", help="run with the default schedule")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--batch-warmup", type=int, default=1)
     ap.add_argument("--batch-legs", default="plain,batched", help="legs of the batched comparison to run")

@@ -169,6 +169,30 @@ rz_status rz_raster_info_build(const rz_geoms* g, uint32_t flags, const uint64_t
 rz_status rz_context_create(int device, rz_context** out, char* err, size_t errlen);
 void rz_context_destroy(rz_context* ctx);
 
+/* The schedule of a context: launch shapes and thresholds of the engine's
+ * kernels that change only its speed, never a result (every setting burns
+ * the same coverage records and folds each pixel's writes in the same
+ * order).  No counterpart in the reference, which has no GPU schedule; the
+ * autotuner (rusterize_gb300.tune) sweeps these per device and workload
+ * class.  A 0 field means the default. */
+typedef struct {
+  uint32_t narrow_chunk;          /* polygon windows per work grab of the narrow span kernel (1..64; 4) */
+  uint32_t narrow_blocks_per_sm;  /* narrow span kernel blocks per SM (1..occupancy limit; the limit) */
+  uint32_t wide_blocks_per_sm;    /* wide span kernel blocks per SM (1..occupancy limit; the limit) */
+  uint32_t rows_per_window;       /* polygon window height cap (8..128; 128) */
+  uint32_t narrow_max_words;      /* widest window of the narrow kernel, in 32-pixel words (1..32; 32) */
+  uint32_t fill_sort_max;         /* records of one tile the warp fill sorts before the per-word path (64..256; 256) */
+  uint32_t scatter_blocks_per_sm; /* record scatter blocks per SM (1..32; 8) */
+  uint32_t line_blocks_per_sm;    /* line and point span kernels, blocks per SM (1..32; 8) */
+} rz_tuning;
+
+/* The settings in force (defaults filled in). */
+rz_status rz_context_get_tuning(rz_context* ctx, rz_tuning* out);
+
+/* Set the schedule (NULL: all defaults).  Values outside their ranges give
+ * RZ_INVALID_ARGUMENT and leave the schedule unchanged. */
+rz_status rz_context_set_tuning(rz_context* ctx, const rz_tuning* tuning, char* err, size_t errlen);
+
 /* Release the context's cached scratch arena (it regrows on demand). */
 rz_status rz_context_trim(rz_context* ctx);
 

@@ -100,6 +100,26 @@ class RzBatchStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class RzTuning(ctypes.Structure):
+    """rz_tuning: the schedule of a context (0 fields: defaults)."""
+
+    _fields_ = [
+        ("narrow_chunk", c_uint32), ("narrow_blocks_per_sm", c_uint32), ("wide_blocks_per_sm", c_uint32),
+        ("rows_per_window", c_uint32), ("narrow_max_words", c_uint32), ("fill_sort_max", c_uint32),
+        ("scatter_blocks_per_sm", c_uint32), ("line_blocks_per_sm", c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "RzTuning":
+        t = cls()
+        for name, _ in cls._fields_:
+            setattr(t, name, int(d.get(name, 0)))
+        return t
+
+
 class RzSparseView(ctypes.Structure):
     _fields_ = [
         ("count", c_uint64), ("n_bands", c_uint32), ("dtype", c_int),
@@ -124,6 +144,8 @@ PROTOTYPES = {
     "rz_context_trim": (c_int, [c_void_p]),
     "rz_context_synchronize": (c_int, [c_void_p, c_char_p, c_size_t]),
     "rz_context_stream": (c_void_p, [c_void_p]),
+    "rz_context_get_tuning": (c_int, [c_void_p, POINTER(RzTuning)]),
+    "rz_context_set_tuning": (c_int, [c_void_p, POINTER(RzTuning), c_char_p, c_size_t]),
     "rz_rasterize": (c_int, [c_void_p, POINTER(RzGeoms), c_void_p, c_void_p, c_void_p, c_uint32,
                              POINTER(RzRasterInfo), c_int, c_int, c_uint32, c_void_p, POINTER(RzStats),
                              c_char_p, c_size_t]),
@@ -221,6 +243,25 @@ class Context:
 
     def trim(self) -> None:
         self._lib.rz_context_trim(self._h)
+
+    @property
+    def tuning(self) -> dict:
+        """The schedule in force (rz_context_get_tuning), defaults filled in."""
+        t = RzTuning()
+        raise_for(self._lib.rz_context_get_tuning(self._h, ctypes.byref(t)), b"rz_context_get_tuning failed")
+        return t.as_dict()
+
+    def set_tuning(self, tuning: dict | None) -> None:
+        """Set the schedule (rz_context_set_tuning); None restores the defaults.
+        Fields left out (or 0) take their defaults."""
+        e = errbuf()
+        with self.lock:
+            if tuning is None:
+                st = self._lib.rz_context_set_tuning(self._h, None, e, len(e))
+            else:
+                t = RzTuning.from_dict(tuning)
+                st = self._lib.rz_context_set_tuning(self._h, ctypes.byref(t), e, len(e))
+        raise_for(st, e.value)
 
     def close(self) -> None:
         if getattr(self, "_h", None):

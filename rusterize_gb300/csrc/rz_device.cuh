@@ -47,6 +47,16 @@ constexpr int SMALL_WARPS = 4;  // warps (independent windows) per block
 constexpr int SMALL_WARP_SMEM = POLY_WARP_QCAP * POLY_QENT + SMALL_BITMAP_WORDS * 4 + 3 * WR_MAX * 4 + 16;
 constexpr int SMALL_SMEM = SMALL_WARPS * SMALL_WARP_SMEM;
 
+// Launch shapes and thresholds that change only the schedule, never a
+// result: every setting burns the same records in the same order per pixel.
+// The context holds one set (rz_tuning in the C ABI); the autotuner picks it.
+struct Tune {
+  int narrow_chunk;      // narrow polygon windows taken per work grab (1..64)
+  int rows_per_window;   // polygon window height cap (8..WR_MAX)
+  int narrow_max_words;  // windows at most this many 32-pixel words wide take the narrow kernel (1..SMALL_BW)
+  int fill_sort_max;     // the warp fill sorts up to this many records of a tile (FILL_WARP_MAX..FILL_WARP_SORT)
+};
+
 // Fill: buckets with at most FILL_WARP_SORT records are sorted and applied by
 // one warp; larger ones go to the per-word path, which takes at most
 // BIG_CAP records of one word at a time.

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <mutex>
 #include <thread>
+#include <unistd.h>
 
 #include "rz_batch.cuh"
 #include "rz_device.cuh"
@@ -100,9 +101,9 @@ fill_fn fill_for(rz_dtype dt) {
   return nullptr;
 }
 
-void launch_scatter(int sms, cudaStream_t s, const RecBuf& sb, const unsigned* boff, unsigned* bcount, uint2* sorted,
-                    Ctrl* ctrl) {
-  k_scatter<<<sms * 8, 256, 0, s>>>(sb, boff, bcount, sorted, ctrl);
+void launch_scatter(int sms, int bps, cudaStream_t s, const RecBuf& sb, const unsigned* boff, unsigned* bcount,
+                    uint2* sorted, Ctrl* ctrl) {
+  k_scatter<<<sms * bps, 256, 0, s>>>(sb, boff, bcount, sorted, ctrl);
 }
 
 // The burn value of every part (values[part_geom[p]], tsize bytes each).
@@ -217,10 +218,37 @@ struct PartTables {
   unsigned long long* last_kept;
 };
 
+// A schedule resolved for one device: the context's rz_tuning with its
+// defaults filled in and clamped to what the kernels allow.
+struct Sched {
+  int sms = 1;
+  int narrow_bps = 1, wide_bps = 1;  // span kernels, blocks per SM
+  int scatter_bps = 8, line_bps = 8;
+  Tune tune{4, WR_MAX, SMALL_BW, FILL_WARP_SORT};
+};
+
+int clamp_i(long v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : (int)v); }
+
+// Defaults for 0 fields; the occupancy limits of the span kernels bound their grids.
+Sched resolve_sched(const rz_tuning& t, int sms, int narrow_occ, int wide_occ) {
+  Sched sc;
+  sc.sms = sms;
+  sc.narrow_bps = t.narrow_blocks_per_sm ? clamp_i(t.narrow_blocks_per_sm, 1, narrow_occ) : narrow_occ;
+  sc.wide_bps = t.wide_blocks_per_sm ? clamp_i(t.wide_blocks_per_sm, 1, wide_occ) : wide_occ;
+  sc.scatter_bps = t.scatter_blocks_per_sm ? clamp_i(t.scatter_blocks_per_sm, 1, 32) : 8;
+  sc.line_bps = t.line_blocks_per_sm ? clamp_i(t.line_blocks_per_sm, 1, 32) : 8;
+  sc.tune.narrow_chunk = t.narrow_chunk ? clamp_i(t.narrow_chunk, 1, 64) : 4;
+  sc.tune.rows_per_window = t.rows_per_window ? clamp_i(t.rows_per_window, 8, WR_MAX) : WR_MAX;
+  sc.tune.narrow_max_words = t.narrow_max_words ? clamp_i(t.narrow_max_words, 1, SMALL_BW) : SMALL_BW;
+  sc.tune.fill_sort_max = t.fill_sort_max ? clamp_i(t.fill_sort_max, FILL_WARP_MAX, FILL_WARP_SORT) : FILL_WARP_SORT;
+  return sc;
+}
+
 // validate -> part -> geometry -> part plans -> scan -> part lists.  Returns
 // the kernels launched.
 int launch_prep(const Geo& geo, const Grid& gr, const JobDims& one, const JobDims* jobs, unsigned n_jobs,
-                unsigned band_check, const PartTables& t, Ctrl* d_ctrl, int sms, cudaStream_t s) {
+                unsigned band_check, const PartTables& t, Ctrl* d_ctrl, const Sched& sc, cudaStream_t s) {
+  const int sms = sc.sms;
   const unsigned long long G = geo.n_geoms, P = geo.n_parts, R = geo.n_rings;
   int launches = 0;
   const unsigned long long maxn = std::max({G + 1, P + 1, R + 1});
@@ -236,7 +264,7 @@ int launch_prep(const Geo& geo, const Grid& gr, const JobDims& one, const JobDim
   }
   if (P) {
     k_part_prep<<<grid_for(P, 8, sms * 32), 256, 0, s>>>(geo, gr, one, jobs, n_jobs, t.part_geom, t.plan, t.counts,
-                                                         d_ctrl);
+                                                         sc.tune, d_ctrl);
     ++launches;
   }
   launches += scan<unsigned long long, PC_N>(t.counts, t.poff, P, t.tmp64, s);
@@ -249,19 +277,21 @@ int launch_prep(const Geo& geo, const Grid& gr, const JobDims& one, const JobDim
 
 // Coverage records of every part kind.  Returns the kernels launched.
 int launch_coverage(const Geo& geo, const Grid& gr, const PartTables& t, const RecBuf& sb, unsigned* bcount,
-                    Ctrl* d_ctrl, int sms, int narrow_bps, int poly_bps, cudaStream_t s) {
+                    Ctrl* d_ctrl, const Sched& sc, cudaStream_t s) {
   if (!geo.n_parts) return 0;
-  k_poly_spans_narrow<<<sms * narrow_bps, SMALL_WARPS * 32, SMALL_SMEM, s>>>(geo, gr, t.plan, t.poff, sb, bcount,
-                                                                             d_ctrl);
-  k_poly_spans<<<sms * poly_bps, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, t.plan, t.poff, sb, bcount, d_ctrl);
-  k_line_spans<<<sms * 8, 256, 0, s>>>(geo, gr, t.plan, t.poff, t.line_parts, t.last_kept, sb, bcount, d_ctrl);
+  const int sms = sc.sms;
+  k_poly_spans_narrow<<<sms * sc.narrow_bps, SMALL_WARPS * 32, SMALL_SMEM, s>>>(geo, gr, t.plan, t.poff, sb, bcount,
+                                                                                sc.tune.narrow_chunk, d_ctrl);
+  k_poly_spans<<<sms * sc.wide_bps, POLY_THREADS, POLY_SMEM, s>>>(geo, gr, t.plan, t.poff, sb, bcount, d_ctrl);
+  k_line_spans<<<sms * sc.line_bps, 256, 0, s>>>(geo, gr, t.plan, t.poff, t.line_parts, t.last_kept, sb, bcount,
+                                                 d_ctrl);
   int launches = 4;
   if (!gr.touched) {  // AllTouched writes no separate end pixel
     k_line_endpix<<<grid_for(geo.n_parts, 256, sms * 4), 256, 0, s>>>(geo, gr, t.plan, t.poff, t.line_parts,
                                                                        t.last_kept, sb, bcount, d_ctrl);
     ++launches;
   }
-  k_point_spans<<<sms * 8, 256, 0, s>>>(geo, gr, t.plan, t.poff, t.point_parts, sb, bcount, d_ctrl);
+  k_point_spans<<<sms * sc.line_bps, 256, 0, s>>>(geo, gr, t.plan, t.poff, t.point_parts, sb, bcount, d_ctrl);
   return launches;
 }
 
@@ -278,8 +308,9 @@ struct rz_sparse {
 struct rz_context {
   int device = 0;
   int num_sms = 0;
-  int poly_blocks_per_sm = 1;
+  int poly_blocks_per_sm = 1;    // occupancy limits of the span kernels
   int narrow_blocks_per_sm = 1;
+  rz_tuning tuning{};            // the schedule (0 fields: defaults)
   cudaStream_t stream = nullptr;
   DevBuf main, spans, out, sparse, batch, stage;
   cudaEvent_t ev[9] = {};
@@ -379,6 +410,49 @@ extern "C" rz_status rz_context_trim(rz_context* ctx) {
   return RZ_OK;
 }
 
+extern "C" rz_status rz_context_get_tuning(rz_context* ctx, rz_tuning* out) {
+  if (!ctx || !out) return RZ_INVALID_ARGUMENT;
+  // the settings in force, defaults filled in
+  const Sched sc = resolve_sched(ctx->tuning, ctx->num_sms, ctx->narrow_blocks_per_sm, ctx->poly_blocks_per_sm);
+  out->narrow_chunk = (uint32_t)sc.tune.narrow_chunk;
+  out->narrow_blocks_per_sm = (uint32_t)sc.narrow_bps;
+  out->wide_blocks_per_sm = (uint32_t)sc.wide_bps;
+  out->rows_per_window = (uint32_t)sc.tune.rows_per_window;
+  out->narrow_max_words = (uint32_t)sc.tune.narrow_max_words;
+  out->fill_sort_max = (uint32_t)sc.tune.fill_sort_max;
+  out->scatter_blocks_per_sm = (uint32_t)sc.scatter_bps;
+  out->line_blocks_per_sm = (uint32_t)sc.line_bps;
+  return RZ_OK;
+}
+
+extern "C" rz_status rz_context_set_tuning(rz_context* ctx, const rz_tuning* t, char* err, size_t errlen) {
+  rz::clear_err(err, errlen);
+  if (!ctx) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null context");
+  if (!t) {
+    ctx->tuning = rz_tuning{};
+    return RZ_OK;
+  }
+  struct Range {
+    const char* name;
+    uint32_t v, lo, hi;
+  };
+  const Range ranges[] = {
+      {"narrow_chunk", t->narrow_chunk, 1, 64},
+      {"narrow_blocks_per_sm", t->narrow_blocks_per_sm, 1, (uint32_t)ctx->narrow_blocks_per_sm},
+      {"wide_blocks_per_sm", t->wide_blocks_per_sm, 1, (uint32_t)ctx->poly_blocks_per_sm},
+      {"rows_per_window", t->rows_per_window, 8, (uint32_t)WR_MAX},
+      {"narrow_max_words", t->narrow_max_words, 1, (uint32_t)SMALL_BW},
+      {"fill_sort_max", t->fill_sort_max, (uint32_t)FILL_WARP_MAX, (uint32_t)FILL_WARP_SORT},
+      {"scatter_blocks_per_sm", t->scatter_blocks_per_sm, 1, 32},
+      {"line_blocks_per_sm", t->line_blocks_per_sm, 1, 32},
+  };
+  for (const Range& r : ranges)
+    if (r.v != 0 && (r.v < r.lo || r.v > r.hi))
+      return fail(err, errlen, RZ_INVALID_ARGUMENT, "%s = %u is outside [%u, %u]", r.name, r.v, r.lo, r.hi);
+  ctx->tuning = *t;
+  return RZ_OK;
+}
+
 extern "C" void* rz_context_stream(rz_context* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
 
 extern "C" rz_status rz_context_synchronize(rz_context* ctx, char* err, size_t errlen) {
@@ -401,6 +475,49 @@ __global__ void k_reset_pass(Ctrl* c) {
 
 // After a failed call: wait for any kernels or copies the call had already
 // queued, so that the caller may free its buffers once the call returns.
+// Host pages of a pageable output that the process has never touched are
+// faulted in (and zeroed by the OS) when the device->host copy first writes
+// them, which slows that copy several-fold.  While the device burns, host
+// threads touch one byte of every page instead, so the copy finds the pages
+// resident.  Pinned or registered outputs are resident already and are left
+// alone; so are outputs below 64 MiB.
+class PageToucher {
+ public:
+  void start(void* out, size_t bytes) {
+    if (!out || bytes < (64u << 20)) return;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, out) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    if (attr.type != cudaMemoryTypeUnregistered) return;  // pinned, registered, device or managed
+    const long pg = sysconf(_SC_PAGESIZE);
+    const size_t page = pg > 0 ? (size_t)pg : 4096;
+    unsigned hw = std::thread::hardware_concurrency();
+    const unsigned n = (unsigned)std::max<size_t>(1, std::min<size_t>({(size_t)(hw ? hw : 1), (size_t)16,
+                                                                         bytes / (32u << 20)}));
+    volatile unsigned char* base = static_cast<volatile unsigned char*>(out);
+    try {
+      for (unsigned t = 0; t < n; ++t) {
+        const size_t lo = bytes / n * t, hi = t + 1 == n ? bytes : bytes / n * (t + 1);
+        threads_.emplace_back([base, lo, hi, page] {
+          // the first byte of every page the slice overlaps
+          for (size_t o = lo - lo % page; o < hi; o += page) base[o < lo ? lo : o] = 0;
+        });
+      }
+    } catch (...) {  // no thread: the copy faults the pages in itself
+    }
+  }
+  void join() {
+    for (auto& t : threads_) t.join();
+    threads_.clear();
+  }
+  ~PageToucher() { join(); }
+
+ private:
+  std::vector<std::thread> threads_;
+};
+
 static rz_status drain_on_error(cudaStream_t s, rz_status st) {
   if (st != RZ_OK && s) {
     cudaStreamSynchronize(s);
@@ -559,6 +676,8 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     geo.bands = band_of_geom;
   }
   if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[8], s));
+  PageToucher toucher;  // joined before the first device->host copy (or on return)
+  if (!out_dev && !sp) toucher.start(out, (size_t)(out_elems * tsize));
 
   const bool touched = (flags & RZ_FLAG_ALL_TOUCHED) != 0;
   const Grid gr = make_grid(info, touched);
@@ -576,6 +695,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   unsigned* boff = static_cast<unsigned*>(at(o_boff));
   unsigned* big = static_cast<unsigned*>(at(o_big));
   const int sms = ctx->num_sms;
+  const Sched sched = resolve_sched(ctx->tuning, sms, ctx->narrow_blocks_per_sm, ctx->poly_blocks_per_sm);
   int launches = 0;
   unsigned reruns = 0;
   const fill_fn fill = fill_for(dt);
@@ -606,7 +726,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     pt.line_parts = line_parts;
     pt.point_parts = point_parts;
     pt.last_kept = last_kept;
-    launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sms, s);
+    launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sched, s);
     if (d_values && !sp && P) {
       launch_part_values(tsize, sms, s, part_geom, d_values, P, at(o_pval), d_ctrl);
       ++launches;
@@ -630,12 +750,11 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
       k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
       RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
       launches += 1;
-      launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sms, ctx->narrow_blocks_per_sm,
-                                  ctx->poly_blocks_per_sm, s);
+      launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sched, s);
       if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[3], s));
       if (!sp) {
         launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
-        launch_scatter(sms, s, sb, boff, bcount, sorted, d_ctrl);
+        launch_scatter(sms, sched.scatter_bps, s, sb, boff, bcount, sorted, d_ctrl);
         ++launches;
         if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
         FillArgs fa;
@@ -652,6 +771,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
         fa.big = big;
         fa.ctrl = d_ctrl;
         fa.rec_cap = cap;
+        fa.sort_max = sched.tune.fill_sort_max;
         fa.work = &d_ctrl->fill_work;
         fa.nbig = &d_ctrl->big_count;
         fa.jobs = nullptr;
@@ -801,6 +921,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
       RZ_CUDA(cudaMemcpyAsync(sp->band_counts.data(), bcnt, 8 * nb, cudaMemcpyDeviceToHost, s));
       if (stats) stats->pixel_writes = total;
     } else if (!out_dev) {
+      toucher.join();
       const size_t bytes = (size_t)((pw.b1 - pw.b0) * (pw.r1 - pw.r0) * ncols * tsize);
       RZ_CUDA(cudaMemcpyAsync(static_cast<char*>(out) + out_off, d_out, bytes, cudaMemcpyDeviceToHost, s));
     }
@@ -1054,6 +1175,7 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   unsigned* boff = static_cast<unsigned*>(at(o_boff));
   unsigned* big = static_cast<unsigned*>(at(o_big));
   const int sms = nd.sms;
+  const Sched sched = resolve_sched(rz_tuning{}, sms, nd.narrow_bps, nd.poly_bps);
   int launches = 0;
 
   RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
@@ -1066,7 +1188,7 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   pt.line_parts = line_parts;
   pt.point_parts = point_parts;
   pt.last_kept = last_kept;
-  launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sms, s);
+  launches += launch_prep(geo, gr, one, nullptr, 1, band_of_geom ? (unsigned)nb : 0u, pt, d_ctrl, sched, s);
   const void* d_vals_na = per_geom_values ? values : nullptr;
   if (d_vals_na && P) {
     launch_part_values(tsize, sms, s, part_geom, d_vals_na, P, at(o_pval), d_ctrl);
@@ -1084,9 +1206,9 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   k_reset_pass<<<1, 1, 0, s>>>(d_ctrl);
   RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * nbuckets, s));
   ++launches;
-  launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sms, nd.narrow_bps, nd.poly_bps, s);
+  launches += launch_coverage(geo, gr, pt, sb, bcount, d_ctrl, sched, s);
   launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
-  launch_scatter(sms, s, sb, boff, bcount, sorted, d_ctrl);
+  launch_scatter(sms, sched.scatter_bps, s, sb, boff, bcount, sorted, d_ctrl);
   ++launches;
   FillArgs fa;
   fa.offsets = boff;
@@ -1102,6 +1224,7 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   fa.big = big;
   fa.ctrl = d_ctrl;
   fa.rec_cap = cap;
+  fa.sort_max = sched.tune.fill_sort_max;
   fa.work = &d_ctrl->fill_work;
   fa.nbig = &d_ctrl->big_count;
   fa.jobs = nullptr;
@@ -1177,6 +1300,7 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
   const bool timing = !(flags & RZ_FLAG_NO_TIMING);
   cudaStream_t s = ctx->stream;
   const int sms = ctx->num_sms;
+  const Sched sched = resolve_sched(ctx->tuning, sms, ctx->narrow_blocks_per_sm, ctx->poly_blocks_per_sm);
   // fill variants contiguous (stable: caller order within a variant)
   std::stable_sort(wave.begin(), wave.end(), [](const BatchJob& a, const BatchJob& b) {
     if (a.fn != b.fn) return a.fn < b.fn;
@@ -1387,7 +1511,7 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
   pt.line_parts = static_cast<unsigned*>(at(o_lp));
   pt.point_parts = static_cast<unsigned*>(at(o_pp));
   pt.last_kept = static_cast<unsigned long long*>(at(o_last));
-  launches += launch_prep(geo, ident, dims[0], d_dims, n, 0u, pt, d_ctrl, sms, s);
+  launches += launch_prep(geo, ident, dims[0], d_dims, n, 0u, pt, d_ctrl, sched, s);
   if (Pt) {  // every job's values are gathered per geometry into the wave table
     launch_part_values(tsize, sms, s, pt.part_geom, w_val, Pt, at(o_pval), d_ctrl);
     ++launches;
@@ -1418,11 +1542,10 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
     RZ_CUDA(cudaMemsetAsync(bcount, 0, 4 * (nbuckets ? nbuckets : 1), s));
     RZ_CUDA(cudaMemsetAsync(gctr, 0, 16 * (n + 1), s));
     ++launches;
-    launches += launch_coverage(geo, ident, pt, sb, bcount, d_ctrl, sms, ctx->narrow_blocks_per_sm,
-                                ctx->poly_blocks_per_sm, s);
+    launches += launch_coverage(geo, ident, pt, sb, bcount, d_ctrl, sched, s);
     if (nbuckets) {
       launches += scan<unsigned, 1>(bcount, boff, nbuckets, static_cast<unsigned*>(at(o_tmp32)), s);
-      launch_scatter(sms, s, sb, boff, bcount, sorted, d_ctrl);
+      launch_scatter(sms, sched.scatter_bps, s, sb, boff, bcount, sorted, d_ctrl);
       ++launches;
       // one fill per variant: a run of jobs with equal (fn, dedup, background)
       unsigned g = 0;
@@ -1446,6 +1569,7 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
           fa.big = big + lo;
           fa.ctrl = d_ctrl;
           fa.rec_cap = cap;
+          fa.sort_max = sched.tune.fill_sort_max;
           fa.work = reinterpret_cast<unsigned long long*>(gctr + 16 * g);
           fa.nbig = reinterpret_cast<unsigned*>(gctr + 16 * g + 8);
           fa.jobs = d_fj;

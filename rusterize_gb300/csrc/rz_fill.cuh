@@ -37,6 +37,7 @@ struct FillArgs {
   unsigned* big;            // buckets left to the per-word kernel
   Ctrl* ctrl;
   unsigned long long rec_cap;
+  int sort_max;              // tiles of up to this many records are sorted by one warp (<= FILL_WARP_SORT)
   unsigned long long* work;  // chunk counter of this fill (zero before the launch)
   unsigned* nbig;            // entries of `big` (zero before the launch)
   // batch calls: bucket b of this fill is bucket bucket0 + b of the call, and
@@ -470,7 +471,7 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
         continue;
       }
       if (n > FILL_WARP_MAX) {
-        if (n > FILL_WARP_SORT) {
+        if (n > a.sort_max) {
           if (lane == 0) a.big[atomicAdd(a.nbig, 1u)] = (unsigned)b;
           continue;
         }

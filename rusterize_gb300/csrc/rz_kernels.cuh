@@ -68,7 +68,7 @@ __global__ void k_part_geom(Geo geo, unsigned* part_geom, Ctrl* ctrl) {
 // line and point parts just report their vertex counts.
 __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restrict__ jobs, unsigned n_jobs,
                             const unsigned* part_geom, PartPlan* plan, unsigned long long* counts /*[P][PC_N]*/,
-                            Ctrl* ctrl) {
+                            Tune tn, Ctrl* ctrl) {
   if (ctrl->err) return;
   const int lane = threadIdx.x & 31;
   const unsigned long long warp0 = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
@@ -180,9 +180,9 @@ __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restr
           const int col0 = (c_lo <= 0.0 ? 0 : (c_lo >= jd.ncols ? jd.ncols : (int)c_lo)) & ~31;
           const int colmax = c_hi <= 0.0 ? 0 : (c_hi >= jd.ncols ? jd.ncols : (int)c_hi);
           const int bw = (colmax - col0 + 1 + 31) >> 5;
-          const bool narrow = bw <= SMALL_BW;
+          const bool narrow = bw <= tn.narrow_max_words;
           int wr = (narrow ? SMALL_BITMAP_WORDS : BITMAP_WORDS) / bw;
-          if (wr > WR_MAX) wr = WR_MAX;
+          if (wr > tn.rows_per_window) wr = tn.rows_per_window;
           if (wr < 1) {
             if (lane == 0) set_error(ctrl, ERR_TOO_WIDE, p);
           } else {

@@ -41,6 +41,8 @@
 // whose warps take contiguous vertex ranges and row ranges of the window.
 #pragma once
 
+#include <climits>
+
 #include "rz_device.cuh"
 
 namespace rzd {
@@ -55,7 +57,6 @@ struct __align__(16) QEnt {
 static_assert(sizeof(QEnt) == 32, "queue entry layout");
 
 constexpr int QCAP = POLY_WARP_QCAP;
-constexpr int NARROW_CHUNK = 4;  // narrow windows per work item
 constexpr int STAGE_CAP = (QCAP * 32) / 12 / 8 * 8;  // staged records per warp (aliases the queue)
 
 struct PolyWin {
@@ -95,18 +96,72 @@ __device__ __noinline__ int cross_exact(const Geo& geo, const Grid& g, unsigned 
   return floor_half_up(x, ncols);                      // floor(x + 0.5) clamped, burners.rs:310-311
 }
 
-// Crossings of the nq queued edges; MODE 0 toggles them in the bitmap, MODE 1
-// records the largest boundary of rows flagged odd.  Lane j of a round takes
-// crossing m0 + j, whose edge is the last one starting at or before it.
-// Every queued edge has at least one row, so edge starts are distinct and one
-// OR-reduction of "start" bits plus a popcount finds it.
+// The queued edge of crossing m0 + lane: the last edge starting at or before
+// it.  Every queued edge has at least one row, so edge starts are distinct
+// and one OR-reduction of "start" bits plus a popcount finds it (edge `lane`
+// has row count n and exclusive row prefix excl).  Returns the edge index in
+// the queue's 32-edge group and sets j to the crossing's row within the edge.
+__device__ __forceinline__ int cross_edge_of(int m0, int n, int excl, int& j) {
+  const int lane = threadIdx.x & 31;
+  const unsigned bit = (n > 0 && excl >= m0 && excl < m0 + 32) ? (1u << (excl - m0)) : 0u;
+  const unsigned starts = __reduce_or_sync(0xFFFFFFFFu, bit);
+  const int before = __popc(__ballot_sync(0xFFFFFFFFu, n > 0 && excl < m0));
+  const int s = before + __popc(starts & ((2u << lane) - 1u)) - 1;
+  const int es = __shfl_sync(0xFFFFFFFFu, excl, s & 31);
+  j = m0 + lane - es;
+  return s;
+}
+
+// The boundary of a crossing (FP32 filter, FP64 fallback), relative to the
+// window's first column, or INT_MIN for a crossing that burns nothing
+// (+NaN); ERR_BITMAP outside the window's bitmap.
+__device__ __forceinline__ int cross_loc(const Geo& geo, const Grid& g, const QEnt& qe, int j, int rowrel,
+                                         unsigned long long vs, const PolyWin& w, Ctrl* ctrl,
+                                         unsigned long long part) {
+  CrossEdge ce;
+  ce.xi = qe.xi;
+  ce.d0 = qe.d0;
+  ce.a = qe.a;
+  ce.c0 = qe.c0;
+  ce.e0 = qe.e0;
+  ce.e1 = qe.e1;
+  int r = cross_fast(ce, j, w.ncols);
+  if (r < 0) {
+    r = cross_exact(geo, g, vs + (qe.v & 0x7FFFFFFFu), qe.v >> 31, w.r0 + rowrel, w.ncols);
+    if (r < 0) return INT_MIN;
+  }
+  const int loc = r - w.col0;
+  if (loc < 0 || loc >= w.nbits) {
+    set_error(ctrl, ERR_BITMAP, part);
+    return INT_MIN;
+  }
+  return loc;
+}
+
+template <int MODE>
+__device__ __forceinline__ void cross_apply(int loc, int rowrel, const PolyWin& w, unsigned* bm, const int* rowslot,
+                                            int* oddmax, unsigned long long& ncross) {
+  if (loc == INT_MIN) return;
+  if (MODE == 0) {
+    atomicXor(&bm[rowrel * w.bw + (loc >> 5)], 1u << (loc & 31));
+    ++ncross;
+  } else if (rowslot[rowrel] >= 0) {
+    atomicMax(&oddmax[rowslot[rowrel]], loc);
+  }
+}
+
+// Crossings of the nq queued edges, dealt to lanes in order over the edges'
+// row counts so that edges with very uneven row spans keep all 32 lanes busy.
+// Two rounds of 32 crossings are taken per iteration, their steps
+// interleaved, so that their latencies overlap.  MODE 0 toggles every
+// boundary in the bitmap; MODE 1 records the largest boundary of rows flagged
+// odd.
 template <int MODE>
 __device__ __forceinline__ void warp_cross(const Geo& geo, const Grid& g, const QEnt* q, int nq,
                                            unsigned long long vs, const PolyWin& w, unsigned* bm,
                                            const int* rowslot, int* oddmax, Ctrl* ctrl, unsigned long long part,
                                            unsigned long long& ncross) {
   const int lane = threadIdx.x & 31;
-  const unsigned lanemask_le = (2u << lane) - 1u;
   for (int base = 0; base < nq; base += 32) {
     const int i = base + lane;
     const int n = i < nq ? (int)(q[i].rows >> 8) : 0;
@@ -118,41 +173,18 @@ __device__ __forceinline__ void warp_cross(const Geo& geo, const Grid& g, const 
     }
     const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     const int excl = incl - n;
-    for (int m0 = 0; m0 < total; m0 += 32) {
-      const unsigned bit = (n > 0 && excl >= m0 && excl < m0 + 32) ? (1u << (excl - m0)) : 0u;
-      const unsigned starts = __reduce_or_sync(0xFFFFFFFFu, bit);
-      const int before = __popc(__ballot_sync(0xFFFFFFFFu, n > 0 && excl < m0));
-      const int s = before + __popc(starts & lanemask_le) - 1;
-      const int es = __shfl_sync(0xFFFFFFFFu, excl, s & 31);
-      const int m = m0 + lane;
-      if (m >= total) continue;
-      const QEnt qe = q[base + s];
-      const int j = m - es;
-      const int rowrel = (int)(qe.rows & 0xFFu) + j;
-      const int row = w.r0 + rowrel;
-      CrossEdge ce;
-      ce.xi = qe.xi;
-      ce.d0 = qe.d0;
-      ce.a = qe.a;
-      ce.c0 = qe.c0;
-      ce.e0 = qe.e0;
-      ce.e1 = qe.e1;
-      int r = cross_fast(ce, j, w.ncols);
-      if (r < 0) {
-        r = cross_exact(geo, g, vs + (qe.v & 0x7FFFFFFFu), qe.v >> 31, row, w.ncols);
-        if (r < 0) continue;
-      }
-      const int loc = r - w.col0;
-      if (loc < 0 || loc >= w.nbits) {
-        set_error(ctrl, ERR_BITMAP, part);
-        continue;
-      }
-      if (MODE == 0) {
-        atomicXor(&bm[rowrel * w.bw + (loc >> 5)], 1u << (loc & 31));
-        ++ncross;
-      } else if (rowslot[rowrel] >= 0) {
-        atomicMax(&oddmax[rowslot[rowrel]], loc);
-      }
+    for (int m0 = 0; m0 < total; m0 += 64) {
+      int ja, jb;
+      const int sa = cross_edge_of(m0, n, excl, ja);
+      const int sb = cross_edge_of(m0 + 32, n, excl, jb);  // past the end: every lane's crossing is >= total
+      const bool ha = m0 + lane < total, hb = m0 + 32 + lane < total;
+      const QEnt qa = q[base + (ha ? sa : 0)];
+      const QEnt qb = q[base + (hb ? sb : 0)];
+      const int ra = (int)(qa.rows & 0xFFu) + ja, rbw = (int)(qb.rows & 0xFFu) + jb;
+      const int la = ha ? cross_loc(geo, g, qa, ja, ra, vs, w, ctrl, part) : INT_MIN;
+      const int lb = hb ? cross_loc(geo, g, qb, jb, rbw, vs, w, ctrl, part) : INT_MIN;
+      cross_apply<MODE>(la, ra, w, bm, rowslot, oddmax, ncross);
+      cross_apply<MODE>(lb, rbw, w, bm, rowslot, oddmax, ncross);
     }
   }
 }
@@ -397,6 +429,70 @@ __device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw,
   }
 }
 
+// Narrow bitmaps (at most ROW_LANE_WORDS words per row): one lane per
+// bitmap row walks the row's words left to right with the running parity of
+// the set bits before each word, so no cross-lane scan is needed.  Each lane
+// then writes its row's records in word order at its place in the warp's
+// stage (a prefix sum of the per-row record counts), which keeps the stage
+// in row-major order like warp_extract.
+constexpr int ROW_LANE_WORDS = 4;
+
+__device__ __forceinline__ void warp_extract_rows(const unsigned* bm, int nr, int bw, int r0, int col0,
+                                                  const PartPlan& pl, unsigned part, WarpScratch& ws, int& st_n,
+                                                  const RecBuf& rb, unsigned* bucket_count, Ctrl* ctrl,
+                                                  unsigned long long& npix) {
+  const int lane = threadIdx.x & 31;
+  const unsigned wpr = pl.wpr;
+  const unsigned w0 = pl.wid0 + ((unsigned)col0 >> 5);
+  const unsigned flags = part | pl.flags;
+  for (int rr = 0; rr < nr; rr += 32) {
+    const int row = rr + lane;
+    const bool valid = row < nr;
+    unsigned cov[ROW_LANE_WORDS];
+    unsigned par = 0u;
+    int cnt = 0;
+#pragma unroll
+    for (int w = 0; w < ROW_LANE_WORDS; ++w) {
+      unsigned c = 0u;
+      if (w < bw && valid) {
+        const unsigned bits = bm[row * bw + w];
+        c = bits;  // inclusive prefix XOR of the word's bits
+        c ^= c << 1;
+        c ^= c << 2;
+        c ^= c << 4;
+        c ^= c << 8;
+        c ^= c << 16;
+        if (par) c = ~c;
+        par ^= (unsigned)__popc(bits) & 1u;
+      }
+      cov[w] = c;
+      cnt += c != 0u;
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    if (total == 0) continue;
+    if (total > STAGE_CAP - st_n) stage_flush(ws, st_n, rb, bucket_count, ctrl);  // total <= 128 < STAGE_CAP
+    int k = st_n + incl - cnt;
+    const unsigned row_wid = (unsigned)(r0 + row) * wpr + w0;
+#pragma unroll
+    for (int w = 0; w < ROW_LANE_WORDS; ++w) {
+      if (cov[w] != 0u) {
+        ws.st_wid[k] = row_wid + (unsigned)w;
+        ws.st_part[k] = flags;
+        ws.st_mask[k] = cov[w];
+        npix += (unsigned long long)__popc(cov[w]);
+        ++k;
+      }
+    }
+    st_n += total;
+  }
+}
+
 // rows of the window with an odd number of crossings (one lane per row)
 __device__ __forceinline__ void warp_find_odd_rows(const unsigned* bm, int rb, int re, int bw, int* rowslot,
                                                    int* oddrow, int* oddmax, int* s_nodd) {
@@ -461,7 +557,7 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
                                                                         const PartPlan* __restrict__ plan,
                                                                         const unsigned long long* __restrict__ poff,
                                                                         RecBuf sb, unsigned* bucket_count,
-                                                                        Ctrl* ctrl) {
+                                                                        int narrow_chunk, Ctrl* ctrl) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned char* base = smem + warp * SMALL_WARP_SMEM;
@@ -478,15 +574,15 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
   int st_n = 0;
   unsigned long long wi = 0, wend = 0, p = 0;
   while (true) {
-    // windows are taken NARROW_CHUNK at a time: the part of the first is
+    // windows are taken narrow_chunk at a time: the part of the first is
     // searched, the following ones walk forward from it
     if (wi >= wend) {
       unsigned long long c0 = 0;
-      if (lane == 0) c0 = atomicAdd(&ctrl->work_small, (unsigned long long)NARROW_CHUNK);
+      if (lane == 0) c0 = atomicAdd(&ctrl->work_small, (unsigned long long)narrow_chunk);
       c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
       if (c0 >= total) break;
       wi = c0;
-      wend = min(total, c0 + NARROW_CHUNK);
+      wend = min(total, c0 + (unsigned long long)narrow_chunk);
       p = window_part(poff, PC_WIN_SMALL, geo.n_parts, wi);
     } else {
       while (poff[(p + 1) * PC_N + PC_WIN_SMALL] <= wi) ++p;
@@ -517,7 +613,10 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
       }
       __syncwarp();
     }
-    warp_extract(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix);
+    if (bw <= ROW_LANE_WORDS)
+      warp_extract_rows(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix);
+    else
+      warp_extract(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix);
     stage_flush(ws, st_n, sb, bucket_count, ctrl);  // the stage aliases the queue of the next window
     ++wi;
   }

@@ -89,6 +89,15 @@ class GeometryTable:
         return GeometryTable(new_po.astype(np.uint64), self.part_kind[parts], new_ro.astype(np.uint64),
                              new_vo.astype(np.uint64), self.ring_flags[rings], self.xy[verts])
 
+    def slice(self, g0: int, g1: int) -> "GeometryTable":
+        """Sub-table of the contiguous geometries [g0, g1), offsets rebased."""
+        p0, p1 = int(self.part_offsets[g0]), int(self.part_offsets[g1])
+        r0, r1 = int(self.ring_offsets[p0]), int(self.ring_offsets[p1])
+        v0, v1 = int(self.vertex_offsets[r0]), int(self.vertex_offsets[r1])
+        return GeometryTable(self.part_offsets[g0:g1 + 1] - np.uint64(p0), self.part_kind[p0:p1],
+                             self.ring_offsets[p0:p1 + 1] - np.uint64(r0), self.vertex_offsets[r0:r1 + 1] - np.uint64(v0),
+                             self.ring_flags[r0:r1], self.xy[v0:v1])
+
     @staticmethod
     def concat(tables: Iterable["GeometryTable"]) -> "GeometryTable":
         tables = list(tables)

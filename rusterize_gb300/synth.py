@@ -59,6 +59,43 @@ def _rings(rng, centres_x, centres_y, radii, counts):
     return xy, sizes
 
 
+def star_polygons_sorted(rng, nv, radius, cx, cy) -> GeometryTable:
+    """Hole-free star polygons, one per entry of the arrays nv (vertex
+    counts), radius and centres, generated without sorting: the n sorted
+    angles of a ring are 2 pi S_k / S_{n+1}, k = 1..n, with S the partial
+    sums of n + 1 standard exponentials -- which has the law of n sorted
+    U[0, 2 pi) draws.  Vertex radius R * U[0.4, 1.0]; each ring is closed."""
+    nv = np.asarray(nv, dtype=np.int64)
+    n = len(nv)
+    k1 = nv + 1                                  # exponentials per ring
+    e = rng.standard_exponential(int(k1.sum()))
+    c = np.cumsum(e)
+    ends = np.cumsum(k1) - 1                     # index of each ring's last exponential
+    starts = ends - nv                           # index of its first
+    base = np.where(starts > 0, c[np.maximum(starts - 1, 0)], 0.0)
+    ring_of = np.repeat(np.arange(n), nv)
+    # positions of the n partial sums S_1..S_n of every ring (its last one is the normaliser)
+    pos = np.arange(int(k1.sum()))
+    keep = np.ones(len(pos), dtype=bool)
+    keep[ends] = False
+    sums = c[keep] - base[ring_of]
+    tot = (c[ends] - base)[ring_of]
+    ang = 2.0 * np.pi * (sums / tot)
+    rad = np.repeat(np.asarray(radius, dtype=np.float64), nv) * rng.uniform(0.4, 1.0, int(nv.sum()))
+    x = np.repeat(np.asarray(cx, dtype=np.float64), nv) + rad * np.cos(ang)
+    y = np.repeat(np.asarray(cy, dtype=np.float64), nv) + rad * np.sin(ang)
+    out_starts = np.concatenate([[0], np.cumsum(k1)[:-1]])
+    xy = np.empty((int(k1.sum()), 2))
+    dst = np.arange(int(nv.sum())) + np.repeat(out_starts - np.concatenate([[0], np.cumsum(nv)[:-1]]), nv)
+    xy[dst, 0] = x
+    xy[dst, 1] = y
+    first = out_starts
+    xy[out_starts + nv] = xy[first]              # closing vertex
+    vo = np.concatenate([[0], np.cumsum(k1)]).astype(np.uint64)
+    ar = np.arange(n + 1, dtype=np.uint64)
+    return GeometryTable(ar, np.full(n, POLYGON, np.uint8), ar, vo, np.zeros(n, np.uint8), xy)
+
+
 def star_polygons(rng, n, nv_range, radius, cx, cy, n_holes=None, hole_nv=(8, 64)) -> GeometryTable:
     """n polygons (one part each) with optional holes."""
     nv = rng.integers(nv_range[0], nv_range[1] + 1, n)
@@ -178,6 +215,50 @@ def mixed(seed: int = 1003, scale: float = 1.0) -> tuple[Workload, Workload]:
 
 
 BATCH_FNS = ("sum", "min", "max", "first", "last", "count")
+
+
+def batch_jobs_fast(seed: int = 1004, n_jobs: int = 4096, side_range: tuple = (256.0, 8192.0),
+                    max_polygons: int = 50_000, chunk: int = 128, threads: int | None = None) -> list[Workload]:
+    """The batch_jobs distributions, generated many jobs at a time: chunks of
+    `chunk` jobs, each from its own stream of SeedSequence(seed) (so the
+    result does not depend on `threads`), built on host threads with
+    star_polygons_sorted over the chunk and split per job.  Same parameters
+    and laws as batch_jobs; different draws, so the jobs differ from
+    batch_jobs(seed)'s."""
+    import concurrent.futures as cf
+    import os
+
+    lo, hi = np.log(side_range[0]), np.log(side_range[1])
+    n_chunks = (n_jobs + chunk - 1) // chunk
+    seeds = np.random.SeedSequence(seed).spawn(max(1, n_chunks))
+
+    def make(ci: int) -> list[Workload]:
+        rng = np.random.default_rng(seeds[ci])
+        c0 = ci * chunk
+        m = min(chunk, n_jobs - c0)
+        npoly = np.clip(np.round(np.exp(np.log(500.0) + rng.normal(0.0, 1.0, m))), 10, max_polygons).astype(np.int64)
+        side = np.round(np.exp(rng.uniform(lo, hi, m)))
+        fns = rng.integers(0, len(BATCH_FNS), m)
+        job_of = np.repeat(np.arange(m), npoly)
+        s_of = side[job_of]
+        radius = np.clip(np.exp(np.log(0.02 * s_of) + rng.normal(0.0, 1.0, len(job_of))), 2.0, 0.25 * s_of)
+        cx, cy = rng.uniform(0.0, 1.0, len(job_of)) * s_of, rng.uniform(0.0, 1.0, len(job_of)) * s_of
+        nv = rng.integers(8, 257, len(job_of))
+        t = star_polygons_sorted(rng, nv, radius, cx, cy)
+        values = rng.uniform(0, 1, len(job_of)).astype(np.float32)
+        g = np.concatenate([[0], np.cumsum(npoly)])
+        out = []
+        for j in range(m):
+            sd = float(side[j])
+            out.append(Workload(f"batch_job_{c0 + j}", t.slice(int(g[j]), int(g[j + 1])),
+                                values[g[j]:g[j + 1]].copy(), (0.0, 0.0, sd, sd), (1.0, 1.0), BATCH_FNS[int(fns[j])],
+                                "float32", float("nan")))
+        return out
+
+    nt = threads or min(16, os.cpu_count() or 1)
+    with cf.ThreadPoolExecutor(max(1, nt)) as ex:
+        parts = list(ex.map(make, range(n_chunks)))
+    return [w for p in parts for w in p]
 
 
 def batch_jobs(seed: int = 1004, n_jobs: int = 4096, side_range: tuple = (256.0, 8192.0),

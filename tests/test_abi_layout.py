@@ -21,6 +21,7 @@ STRUCTS = {
     "rz_sparse_view": _lib.RzSparseView,
     "rz_job": _lib.RzJob,
     "rz_batch_stats": _lib.RzBatchStats,
+    "rz_tuning": _lib.RzTuning,
 }
 
 

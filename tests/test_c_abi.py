@@ -1,8 +1,10 @@
 """The C ABI from C: a program compiled against include/rusterize_gb300.h and
 linked to librusterize_gb300.so (as a Rust, Go or C caller would bind it)
 parses WKT, builds the raster grid, and creates a context.  Without a GPU
-the context call must fail with RZ_NO_DEVICE and a message; with one, it
-succeeds.  CPU test (runs wherever the library is built)."""
+the context call must fail with RZ_NO_DEVICE and a message (CPU test); with
+one, the program burns the geometry with rz_rasterize and with
+rz_rasterize_rows from host buffers and prints both rasters, which must
+equal the oracle's (GPU test)."""
 
 import shutil
 import subprocess
@@ -41,8 +43,27 @@ int main(void) {
   rz_context* ctx = NULL;
   rz_status st = rz_context_create(0, &ctx, err, sizeof err);
   if (st == RZ_OK) {
-    rz_context_destroy(ctx);
     printf("context ok\n");
+    /* sum of per-geometry values (u8) with background 0 */
+    unsigned char vals[2] = {3, 5}, bg = 0;
+    unsigned char out[9 * 11], rows[4 * 11];
+    rz_stats stats;
+    if (info.nrows != 9 || info.ncols != 11) return 18;
+    if (rz_rasterize(ctx, &g, vals, &bg, NULL, 1, &info, RZ_SUM, RZ_U8, 0, out, &stats, err, sizeof err) != RZ_OK) {
+      printf("rasterize failed: %s\n", err);
+      return 19;
+    }
+    if (rz_rasterize_rows(ctx, &g, vals, &bg, NULL, 1, &info, 3, 7, RZ_SUM, RZ_U8, 0, rows, &stats, err,
+                          sizeof err) != RZ_OK) {
+      printf("rasterize_rows failed: %s\n", err);
+      return 20;
+    }
+    printf("raster");
+    for (int i = 0; i < 9 * 11; ++i) printf(" %d", out[i]);
+    printf("\nrows");
+    for (int i = 0; i < 4 * 11; ++i) printf(" %d", rows[i]);
+    printf("\n");
+    rz_context_destroy(ctx);
   } else {
     printf("context %d %s\n", (int)st, err);
   }
@@ -52,13 +73,11 @@ int main(void) {
 """
 
 
-def test_c_program_uses_the_abi(tmp_path):
+def _run_program(tmp_path):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    import rusterize_gb300 as rz
     from rusterize_gb300 import _build
-    from rusterize_gb300 import geometry as G
 
     _lib.load()  # builds the library if needed
     so = _build.lib_path()
@@ -69,7 +88,14 @@ def test_c_program_uses_the_abi(tmp_path):
                     f"-Wl,-rpath,{so.parent}"], check=True)
     res = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert res.returncode == 0, (res.returncode, res.stdout, res.stderr)
-    lines = res.stdout.splitlines()
+    return res.stdout.splitlines()
+
+
+def test_c_program_uses_the_abi(tmp_path):
+    import rusterize_gb300 as rz
+    from rusterize_gb300 import geometry as G
+
+    lines = _run_program(tmp_path)
     # the grid the builder infers from C equals the one the Python front end gets
     t = G.from_wkt(["POLYGON ((0 0, 10 0, 10 5, 0 5, 0 0))", "POINT (2.5 7.5)"])
     i = rz.raster_info(t, res=(1.0, 1.0))
@@ -78,3 +104,24 @@ def test_c_program_uses_the_abi(tmp_path):
     if lines[1] != "context ok":  # no GPU here: the engine refuses, with its message
         assert lines[1].startswith(f"context {_lib.RZ_NO_DEVICE} ")
         assert "no CPU fallback" in lines[1]
+
+
+@pytest.mark.gpu
+def test_c_program_burns_through_the_abi(tmp_path):
+    import numpy as np
+
+    import rusterize_gb300 as rz
+    from rusterize_gb300 import geometry as G
+
+    from _util import oracle_burn
+
+    lines = _run_program(tmp_path)
+    assert lines[1] == "context ok", lines
+    t = G.from_wkt(["POLYGON ((0 0, 10 0, 10 5, 0 5, 0 0))", "POINT (2.5 7.5)"])
+    info = rz.raster_info(t, res=(1.0, 1.0))
+    ref = oracle_burn(t, info, fn="sum", values=np.array([3, 5], np.uint8), background=0, dtype="uint8")[0]
+    got = np.array([int(v) for v in lines[2].split()[1:]], np.uint8).reshape(9, 11)
+    rows = np.array([int(v) for v in lines[3].split()[1:]], np.uint8).reshape(4, 11)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(rows, ref[3:7])
+    assert got.sum() > 0
