@@ -297,6 +297,11 @@ int launch_coverage(const Geo& geo, const Grid& gr, const PartTables& t, const R
 
 }  // namespace
 
+// A dense burn into host memory runs its fill in this many row bands, and
+// copies each band to the host on the context's copy stream while the next
+// band fills.
+constexpr int kFillBands = 8;
+
 // Host copy of a sparse (COO) result.
 struct rz_sparse {
   std::vector<uint64_t> band_counts, rows, cols;
@@ -312,6 +317,8 @@ struct rz_context {
   int narrow_blocks_per_sm = 1;
   rz_tuning tuning{};            // the schedule (0 fields: defaults)
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // device->host copies that overlap the fill
+  cudaEvent_t band_ev[kFillBands + 1] = {};
   DevBuf main, spans, out, sparse, batch, stage;
   cudaEvent_t ev[9] = {};
   Ctrl* h_ctrl = nullptr;  // pinned
@@ -354,6 +361,9 @@ extern "C" rz_status rz_context_create(int device, rz_context** out, char* err, 
   cudaError_t e2 = cudaSetDevice(device);
   if (e2 == cudaSuccess) e2 = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e2 == cudaSuccess) e2 = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e2 == cudaSuccess) e2 = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+  for (int i = 0; i <= kFillBands && e2 == cudaSuccess; ++i)
+    e2 = cudaEventCreateWithFlags(&ctx->band_ev[i], cudaEventDisableTiming);
   for (int i = 0; i < 9 && e2 == cudaSuccess; ++i) e2 = cudaEventCreate(&ctx->ev[i]);
   if (e2 == cudaSuccess) e2 = cudaMallocHost((void**)&ctx->h_ctrl, sizeof(Ctrl));
   if (e2 == cudaSuccess)
@@ -386,11 +396,15 @@ extern "C" void rz_context_destroy(rz_context* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->main, &ctx->spans, &ctx->out, &ctx->sparse, &ctx->batch, &ctx->stage})
     if (b->p) cudaFree(b->p);
+  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
   for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : ctx->band_ev)
     if (e) cudaEventDestroy(e);
   if (ctx->h_ctrl) cudaFreeHost(ctx->h_ctrl);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   delete ctx;
 }
 
@@ -637,6 +651,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
   const size_t o_tmp32 = L.take(4 * scan_temp_elems(max_buckets, 1));
   const size_t o_big = L.take(4 * max_buckets);
   const size_t o_ctrl = L.take(sizeof(Ctrl));
+  const size_t o_bandctr = L.take(16 * kFillBands);  // work / big counters of the fill bands
   RZ_CUDA(ensure(ctx->main, L.off));
   if (!out_dev && !sp) RZ_CUDA(ensure(ctx->out, pass_elems * tsize));
   unsigned long long cap = rzl::record_cap_request(std::max<unsigned long long>(ctx->span_cap_hint, 2 * V + (1ull << 20)));
@@ -733,6 +748,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
     }
     RZ_CUDA(cudaMemsetAsync(last_kept, 0, 8 * (P ? P : 1), s));
     if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[2], s));
+    bool copied = false;  // the fill bands copied the pass's slab to the host
 
     while (true) {
       RZ_CUDA(ensure(ctx->spans, rzl::record_bytes_for(cap)));
@@ -777,13 +793,47 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
         fa.jobs = nullptr;
         fa.n_jobs = 0;
         fa.bucket0 = 0;
-        launches += fill(fa, (int)fn, dedup, sms, s);
+        // one pass into host memory: fill row bands, then copy each band to
+        // the host on the copy stream as soon as its fill is done
+        const unsigned long long brows = (pw.b1 - pw.b0) * (pw.r1 - pw.r0);  // rows of the band stack
+        const int nbands = (!out_dev && passes.size() == 1 && brows >= (unsigned long long)kFillBands * 64)
+                               ? kFillBands : 1;
+        if (nbands == 1) {
+          launches += fill(fa, (int)fn, dedup, sms, s);
+        } else {
+          unsigned char* bctr = static_cast<unsigned char*>(at(o_bandctr));
+          RZ_CUDA(cudaMemsetAsync(bctr, 0, 16 * kFillBands, s));
+          for (int k = 0; k < nbands; ++k) {
+            const unsigned long long r_lo = brows * k / nbands, r_hi = brows * (k + 1) / nbands;
+            FillArgs fb = fa;
+            fb.offsets = boff + r_lo * ntx;
+            fb.nbuckets = (r_hi - r_lo) * ntx;
+            fb.bucket0 = r_lo * ntx;
+            fb.big = big + r_lo * ntx;
+            fb.work = reinterpret_cast<unsigned long long*>(bctr + 16 * k);
+            fb.nbig = reinterpret_cast<unsigned*>(bctr + 16 * k + 8);
+            launches += fill(fb, (int)fn, dedup, sms, s);
+            RZ_CUDA(cudaEventRecord(ctx->band_ev[k], s));
+          }
+          toucher.join();  // the host pages are resident before the first copy
+          const size_t row_bytes = (size_t)ncols * tsize;
+          for (int k = 0; k < nbands; ++k) {
+            const unsigned long long r_lo = brows * k / nbands, r_hi = brows * (k + 1) / nbands;
+            RZ_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->band_ev[k], 0));
+            RZ_CUDA(cudaMemcpyAsync(static_cast<char*>(out) + out_off + r_lo * row_bytes,
+                                    static_cast<char*>(d_out) + r_lo * row_bytes, (r_hi - r_lo) * row_bytes,
+                                    cudaMemcpyDeviceToHost, ctx->copy_stream));
+          }
+          RZ_CUDA(cudaEventRecord(ctx->band_ev[kFillBands], ctx->copy_stream));
+          copied = true;
+        }
       }
       RZ_CUDA(cudaGetLastError());
       if (timing) {
         if (sp) RZ_CUDA(cudaEventRecord(ctx->ev[4], s));
         RZ_CUDA(cudaEventRecord(ctx->ev[5], s));
       }
+      if (copied) RZ_CUDA(cudaStreamWaitEvent(s, ctx->band_ev[kFillBands], 0));  // the band copies are done
       RZ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
       RZ_CUDA(cudaStreamSynchronize(s));
       const Ctrl& hc = *ctx->h_ctrl;
@@ -920,7 +970,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
       }
       RZ_CUDA(cudaMemcpyAsync(sp->band_counts.data(), bcnt, 8 * nb, cudaMemcpyDeviceToHost, s));
       if (stats) stats->pixel_writes = total;
-    } else if (!out_dev) {
+    } else if (!out_dev && !copied) {
       toucher.join();
       const size_t bytes = (size_t)((pw.b1 - pw.b0) * (pw.r1 - pw.r0) * ncols * tsize);
       RZ_CUDA(cudaMemcpyAsync(static_cast<char*>(out) + out_off, d_out, bytes, cudaMemcpyDeviceToHost, s));

@@ -40,15 +40,16 @@ struct FillArgs {
   int sort_max;              // tiles of up to this many records are sorted by one warp (<= FILL_WARP_SORT)
   unsigned long long* work;  // chunk counter of this fill (zero before the launch)
   unsigned* nbig;            // entries of `big` (zero before the launch)
-  // batch calls: bucket b of this fill is bucket bucket0 + b of the call, and
-  // its raster is that of the job owning it; jobs == nullptr: out / ncols / ntx
+  // bucket b of this fill is bucket bucket0 + b of the call (a fill may run
+  // over a sub-range of the buckets); batch calls: its raster is that of the
+  // job owning it; jobs == nullptr: out / ncols / ntx
   const FillJob* jobs;
   unsigned n_jobs;
   unsigned long long bucket0;
 };
 
 __device__ __forceinline__ unsigned long long gb_of(const FillArgs& a, unsigned long long b) {
-  return a.jobs ? a.bucket0 + b : b;
+  return a.bucket0 + b;
 }
 
 // The raster tile of bucket b: its first pixel and its width (the last tile
@@ -76,7 +77,7 @@ __device__ __forceinline__ T* bucket_tile(const FillArgs& a, unsigned long long 
     nrows = a.nrows;  // all bands: rows of the (bands * nrows) stack
     ncols = a.ncols;
     ntx = a.ntx;
-    lb = (unsigned)b;
+    lb = (unsigned)(a.bucket0 + b);  // a fill of a sub-range starts at bucket bucket0
   }
   const unsigned rowid = lb / ntx;  // 32-bit: a 64-bit divide runs on the FP64 pipe
   const int c0 = (int)(lb - rowid * ntx) << TW_SHIFT;

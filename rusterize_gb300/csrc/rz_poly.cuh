@@ -429,70 +429,6 @@ __device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw,
   }
 }
 
-// Narrow bitmaps (at most ROW_LANE_WORDS words per row): one lane per
-// bitmap row walks the row's words left to right with the running parity of
-// the set bits before each word, so no cross-lane scan is needed.  Each lane
-// then writes its row's records in word order at its place in the warp's
-// stage (a prefix sum of the per-row record counts), which keeps the stage
-// in row-major order like warp_extract.
-constexpr int ROW_LANE_WORDS = 4;
-
-__device__ __forceinline__ void warp_extract_rows(const unsigned* bm, int nr, int bw, int r0, int col0,
-                                                  const PartPlan& pl, unsigned part, WarpScratch& ws, int& st_n,
-                                                  const RecBuf& rb, unsigned* bucket_count, Ctrl* ctrl,
-                                                  unsigned long long& npix) {
-  const int lane = threadIdx.x & 31;
-  const unsigned wpr = pl.wpr;
-  const unsigned w0 = pl.wid0 + ((unsigned)col0 >> 5);
-  const unsigned flags = part | pl.flags;
-  for (int rr = 0; rr < nr; rr += 32) {
-    const int row = rr + lane;
-    const bool valid = row < nr;
-    unsigned cov[ROW_LANE_WORDS];
-    unsigned par = 0u;
-    int cnt = 0;
-#pragma unroll
-    for (int w = 0; w < ROW_LANE_WORDS; ++w) {
-      unsigned c = 0u;
-      if (w < bw && valid) {
-        const unsigned bits = bm[row * bw + w];
-        c = bits;  // inclusive prefix XOR of the word's bits
-        c ^= c << 1;
-        c ^= c << 2;
-        c ^= c << 4;
-        c ^= c << 8;
-        c ^= c << 16;
-        if (par) c = ~c;
-        par ^= (unsigned)__popc(bits) & 1u;
-      }
-      cov[w] = c;
-      cnt += c != 0u;
-    }
-    int incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-      if (lane >= o) incl += t;
-    }
-    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    if (total == 0) continue;
-    if (total > STAGE_CAP - st_n) stage_flush(ws, st_n, rb, bucket_count, ctrl);  // total <= 128 < STAGE_CAP
-    int k = st_n + incl - cnt;
-    const unsigned row_wid = (unsigned)(r0 + row) * wpr + w0;
-#pragma unroll
-    for (int w = 0; w < ROW_LANE_WORDS; ++w) {
-      if (cov[w] != 0u) {
-        ws.st_wid[k] = row_wid + (unsigned)w;
-        ws.st_part[k] = flags;
-        ws.st_mask[k] = cov[w];
-        npix += (unsigned long long)__popc(cov[w]);
-        ++k;
-      }
-    }
-    st_n += total;
-  }
-}
-
 // rows of the window with an odd number of crossings (one lane per row)
 __device__ __forceinline__ void warp_find_odd_rows(const unsigned* bm, int rb, int re, int bw, int* rowslot,
                                                    int* oddrow, int* oddmax, int* s_nodd) {
@@ -613,10 +549,7 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
       }
       __syncwarp();
     }
-    if (bw <= ROW_LANE_WORDS)
-      warp_extract_rows(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix);
-    else
-      warp_extract(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix);
+    warp_extract(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix);
     stage_flush(ws, st_n, sb, bucket_count, ctrl);  // the stage aliases the queue of the next window
     ++wi;
   }
