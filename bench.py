@@ -547,7 +547,7 @@ def _served_leg(args, local) -> dict:
             r = None
             try:
                 r = f.result()
-            except BaseException as e:  # a failed request still ends
+            except BaseException as e:  # a failed or cancelled request still ends
                 with lock:
                     errors.append(repr(e)[:200])
             with lock:
@@ -561,6 +561,7 @@ def _served_leg(args, local) -> dict:
                 done.set()
 
         closed = [False]
+        cancelled = [0]
         srv = BurnServer(device=local, budget_bytes=budget, streams=2 if batched else 1,
                          max_batch=args.serve_max_batch if batched else 1)
         try:
@@ -583,19 +584,23 @@ def _served_leg(args, local) -> dict:
                 closed[0] = True
                 if len(lat) + len(errors) == n_sub[0]:
                     done.set()
-            done.wait(300)
+            # a saturated server's backlog is cut off after the drain limit:
+            # what has not started by then is cancelled and reported
+            if not done.wait(args.serve_drain_limit):
+                cancelled[0] = srv.cancel_pending()
+                done.wait(600)
             t_end = time.perf_counter()
             batches = srv.batches
         finally:
             srv.close()
         a = np.array(lat) * 1e3
-        if errors:
-            print(f"served leg: {len(errors)} failed requests, first: {errors[0]}", file=sys.stderr)
-        return {"submitted": n_sub[0], "completed": len(lat), "failed": len(errors),
+        if len(errors) > cancelled[0]:
+            print(f"served leg: {len(errors) - cancelled[0]} failed requests, first: {errors[0]}", file=sys.stderr)
+        return {"submitted": n_sub[0], "completed": len(lat), "failed": len(errors) - cancelled[0],
                 "jobs_per_s": len(lat) / (t_end - t0), "px_per_s": px_done[0] / (t_end - t0),
                 "p50_ms": float(np.percentile(a, 50)) if len(a) else None,
                 "p99_ms": float(np.percentile(a, 99)) if len(a) else None, "batches": batches,
-                "drain_s": t_end - t0 - args.serve_seconds}
+                "drain_s": t_end - t0 - args.serve_seconds, "cancelled_after_drain_limit": cancelled[0]}
 
     rates = []
     for rate in [float(r) for r in args.serve_rates.split(",") if r]:
@@ -634,6 +639,8 @@ def main():
     ap.add_argument("--serve-pool", type=int, default=96)
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)
     ap.add_argument("--serve-max-batch", type=int, default=512)
+    ap.add_argument("--serve-drain-limit", type=float, default=60.0,
+                    help="seconds to wait for the backlog after the arrival window before cancelling it")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -133,6 +133,14 @@ class Admission:
             self.closing = True
             self._cv.notify_all()
 
+    def cancel_pending(self) -> list:
+        """Remove and return the requests that have not been taken yet."""
+        with self._cv:
+            out = list(self._pending)
+            self._pending.clear()
+            self._cv.notify_all()
+            return out
+
     def __len__(self) -> int:
         with self._cv:
             return len(self._pending)
@@ -170,6 +178,16 @@ class BurnServer:
         fut: Future = Future()
         self.admission.put(Request(job, dtype, nbytes, fut, time.perf_counter()))
         return fut
+
+    def cancel_pending(self) -> int:
+        """Fail every request that has not started (its future raises
+        CancelledError); running batches finish.  Returns how many."""
+        from concurrent.futures import CancelledError
+
+        reqs = self.admission.cancel_pending()
+        for r in reqs:
+            r.future.set_exception(CancelledError("request cancelled before it started"))
+        return len(reqs)
 
     def close(self) -> None:
         """Finish the queued requests and stop the schedulers."""

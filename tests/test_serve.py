@@ -34,6 +34,19 @@ def test_admission_takes_the_oldest_dtype_in_order_within_the_budget():
     assert a.take() == []
 
 
+def test_admission_cancel_pending_keeps_reservations_of_taken_batches():
+    a = Admission(budget_bytes=100, max_batch=10)
+    reqs = [_req(60), _req(60), _req(10, "uint8")]
+    for r in reqs:
+        a.put(r)
+    assert a.take() == [reqs[0]] and a.reserved == 60
+    gone = a.cancel_pending()
+    assert gone == [reqs[1], reqs[2]] and len(a) == 0
+    assert a.reserved == 60  # the running batch still holds its bytes
+    a.release(60)
+    assert a.take(timeout=0.05) == [] and a.reserved == 0
+
+
 def test_admission_rejects_requests_beyond_the_budget_and_after_close():
     a = Admission(budget_bytes=100, max_batch=10)
     with pytest.raises(ValueError, match="budget"):
