@@ -534,7 +534,7 @@ def _served_leg(args, local) -> dict:
         pool.append((BatchJob(DeviceTable.upload(w.table, device=local), info, upload(vals, device=local), w.fn, bg),
                      dtype))
     free, _ = torch.cuda.mem_get_info(local)
-    budget = int(min(args.serve_budget_gb * (1 << 30), 0.4 * free))
+    budget = int(min(args.serve_budget_gb * (1 << 30), 0.5 * free))
 
     def run(rate, batched):
         rng = np.random.default_rng(int(rate) * 7 + batched)
@@ -591,6 +591,7 @@ def _served_leg(args, local) -> dict:
                 done.wait(600)
             t_end = time.perf_counter()
             batches = srv.batches
+            dev_ms, call_ms = srv.device_ms, srv.call_ms
         finally:
             srv.close()
         a = np.array(lat) * 1e3
@@ -600,7 +601,9 @@ def _served_leg(args, local) -> dict:
                 "jobs_per_s": len(lat) / (t_end - t0), "px_per_s": px_done[0] / (t_end - t0),
                 "p50_ms": float(np.percentile(a, 50)) if len(a) else None,
                 "p99_ms": float(np.percentile(a, 99)) if len(a) else None, "batches": batches,
-                "drain_s": t_end - t0 - args.serve_seconds, "cancelled_after_drain_limit": cancelled[0]}
+                "drain_s": t_end - t0 - args.serve_seconds, "cancelled_after_drain_limit": cancelled[0],
+                "device_ms": dev_ms, "batch_call_ms": call_ms,
+                "device_busy": dev_ms / 1e3 / (t_end - t0) / (2 if batched else 1)}
 
     rates = []
     for rate in [float(r) for r in args.serve_rates.split(",") if r]:

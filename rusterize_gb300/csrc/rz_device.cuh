@@ -36,6 +36,11 @@ constexpr uint32_t DEDUP_BIT = 1u << 31;
 // Narrow parts (bitmap row <= SMALL_BW words) take one warp per window with
 // a small bitmap; wider parts take one block per window.
 constexpr int BITMAP_WORDS = 8192;
+// Parts wider than BITMAP_WORDS words take column windows of COLWIN_WORDS
+// words and COLWIN_ROWS rows; a crossing left of a column window only flips
+// its row's parity, one right of it is only counted.
+constexpr int COLWIN_WORDS = 1024;
+constexpr int COLWIN_ROWS = BITMAP_WORDS / COLWIN_WORDS;
 constexpr int WR_MAX = 128;                 // rows per window
 constexpr int POLY_THREADS = 256;
 constexpr int POLY_QENT = 32;               // bytes of one queued edge
@@ -147,7 +152,7 @@ struct PartPlan {
   unsigned wpr;      // record words per raster row (ntx * WPT)
   unsigned flags;    // flags of the part's records (DEDUP_BIT)
   int rlo, rhi;      // rows of the window: pixels outside are not written
-  unsigned pad;
+  unsigned ncw;      // column windows (0: one window spans the part's columns)
 };
 
 // Part-level counters, scanned (exclusive) into offsets: polygon windows of

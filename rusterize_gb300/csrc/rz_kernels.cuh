@@ -94,7 +94,7 @@ __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restr
     pl.flags = kind == 1 ? jd.line_flag : (kind == 2 ? jd.poly_flag : 0u);
     pl.rlo = jd.row_lo;
     pl.rhi = jd.row_hi;
-    pl.pad = 0;
+    pl.ncw = 0;
     // parts of bands outside the window burn nothing in this call
     const bool in_window = band >= jd.band_lo && band < jd.band_hi && jd.row_lo < jd.row_hi;
     if (!in_window) {
@@ -142,13 +142,17 @@ __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restr
           nan_x = 1;
         }
       };
-      // two loads in flight per lane; min / max are idempotent, so a missing
-      // second vertex folds the first one again
-      for (unsigned long long v = vs + lane; v < ve; v += 64) {
+      // four loads in flight per lane; min / max are idempotent, so a
+      // missing vertex folds the first one again
+      for (unsigned long long v = vs + lane; v < ve; v += 128) {
         const double2 w = geo.xy[v];
         const double2 w2 = v + 32 < ve ? geo.xy[v + 32] : w;
+        const double2 w3 = v + 64 < ve ? geo.xy[v + 64] : w;
+        const double2 w4 = v + 96 < ve ? geo.xy[v + 96] : w;
         fold(w);
         fold(w2);
+        fold(w3);
+        fold(w4);
       }
       for (int o = 16; o > 0; o >>= 1) {
         ylo = min(ylo, (long long)__shfl_xor_sync(0xFFFFFFFFu, (unsigned long long)ylo, o));
@@ -181,15 +185,18 @@ __global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restr
           const int colmax = c_hi <= 0.0 ? 0 : (c_hi >= jd.ncols ? jd.ncols : (int)c_hi);
           const int bw = (colmax - col0 + 1 + 31) >> 5;
           const bool narrow = bw <= tn.narrow_max_words;
-          int wr = (narrow ? SMALL_BITMAP_WORDS : BITMAP_WORDS) / bw;
-          if (wr > tn.rows_per_window) wr = tn.rows_per_window;
-          if (wr < 1) {
-            if (lane == 0) set_error(ctrl, ERR_TOO_WIDE, p);
+          pl.row0 = row0;
+          pl.row1 = row1;
+          pl.col0 = col0;
+          pl.bw = bw;
+          if (bw > BITMAP_WORDS) {  // wider than one bitmap: windows of columns too
+            const int wr = min(COLWIN_ROWS, tn.rows_per_window);
+            pl.wr = wr;
+            pl.ncw = (unsigned)((bw + COLWIN_WORDS - 1) / COLWIN_WORDS);
+            c[PC_WINDOWS] = (unsigned long long)((row1 - row0 + wr - 1) / wr) * pl.ncw;
           } else {
-            pl.row0 = row0;
-            pl.row1 = row1;
-            pl.col0 = col0;
-            pl.bw = bw;
+            int wr = (narrow ? SMALL_BITMAP_WORDS : BITMAP_WORDS) / bw;
+            if (wr > tn.rows_per_window) wr = tn.rows_per_window;
             pl.wr = wr;
             c[narrow ? PC_WIN_SMALL : PC_WINDOWS] = (unsigned long long)((row1 - row0 + wr - 1) / wr);
           }

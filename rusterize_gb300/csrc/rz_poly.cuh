@@ -62,6 +62,7 @@ constexpr int STAGE_CAP = (QCAP * 32) / 12 / 8 * 8;  // staged records per warp 
 struct PolyWin {
   int r0, r1, col0, nbits, bw;
   int nrows, ncols;  // the part's raster
+  bool colwin;       // a column window: crossings may fall left or right of it
 };
 
 // Per-warp shared-memory scratch: the edge queue, which doubles as the
@@ -115,6 +116,7 @@ __device__ __forceinline__ int cross_edge_of(int m0, int n, int excl, int& j) {
 // The boundary of a crossing (FP32 filter, FP64 fallback), relative to the
 // window's first column, or INT_MIN for a crossing that burns nothing
 // (+NaN); ERR_BITMAP outside the window's bitmap.
+template <bool COLW>
 __device__ __forceinline__ int cross_loc(const Geo& geo, const Grid& g, const QEnt& qe, int j, int rowrel,
                                          unsigned long long vs, const PolyWin& w, Ctrl* ctrl,
                                          unsigned long long part) {
@@ -131,19 +133,23 @@ __device__ __forceinline__ int cross_loc(const Geo& geo, const Grid& g, const QE
     if (r < 0) return INT_MIN;
   }
   const int loc = r - w.col0;
-  if (loc < 0 || loc >= w.nbits) {
+  if (!(COLW && w.colwin) && (loc < 0 || loc >= w.nbits)) {
     set_error(ctrl, ERR_BITMAP, part);
     return INT_MIN;
   }
   return loc;
 }
 
-template <int MODE>
+// A column window's crossings left of it flip its row's carry (bit 0 of
+// `side`), those right of it flip bit 1: only the parity of each matters.
+template <int MODE, bool COLW>
 __device__ __forceinline__ void cross_apply(int loc, int rowrel, const PolyWin& w, unsigned* bm, const int* rowslot,
-                                            int* oddmax, unsigned long long& ncross) {
+                                            int* oddmax, unsigned* side, unsigned long long& ncross) {
   if (loc == INT_MIN) return;
   if (MODE == 0) {
-    atomicXor(&bm[rowrel * w.bw + (loc >> 5)], 1u << (loc & 31));
+    if (COLW && loc < 0) atomicXor(&side[rowrel], 1u);
+    else if (COLW && loc >= w.nbits) atomicXor(&side[rowrel], 2u);
+    else atomicXor(&bm[rowrel * w.bw + (loc >> 5)], 1u << (loc & 31));
     ++ncross;
   } else if (rowslot[rowrel] >= 0) {
     atomicMax(&oddmax[rowslot[rowrel]], loc);
@@ -156,11 +162,11 @@ __device__ __forceinline__ void cross_apply(int loc, int rowrel, const PolyWin& 
 // interleaved, so that their latencies overlap.  MODE 0 toggles every
 // boundary in the bitmap; MODE 1 records the largest boundary of rows flagged
 // odd.
-template <int MODE>
+template <int MODE, bool COLW>
 __device__ __forceinline__ void warp_cross(const Geo& geo, const Grid& g, const QEnt* q, int nq,
                                            unsigned long long vs, const PolyWin& w, unsigned* bm,
-                                           const int* rowslot, int* oddmax, Ctrl* ctrl, unsigned long long part,
-                                           unsigned long long& ncross) {
+                                           const int* rowslot, int* oddmax, unsigned* side, Ctrl* ctrl,
+                                           unsigned long long part, unsigned long long& ncross) {
   const int lane = threadIdx.x & 31;
   for (int base = 0; base < nq; base += 32) {
     const int i = base + lane;
@@ -181,10 +187,10 @@ __device__ __forceinline__ void warp_cross(const Geo& geo, const Grid& g, const 
       const QEnt qa = q[base + (ha ? sa : 0)];
       const QEnt qb = q[base + (hb ? sb : 0)];
       const int ra = (int)(qa.rows & 0xFFu) + ja, rbw = (int)(qb.rows & 0xFFu) + jb;
-      const int la = ha ? cross_loc(geo, g, qa, ja, ra, vs, w, ctrl, part) : INT_MIN;
-      const int lb = hb ? cross_loc(geo, g, qb, jb, rbw, vs, w, ctrl, part) : INT_MIN;
-      cross_apply<MODE>(la, ra, w, bm, rowslot, oddmax, ncross);
-      cross_apply<MODE>(lb, rbw, w, bm, rowslot, oddmax, ncross);
+      const int la = ha ? cross_loc<COLW>(geo, g, qa, ja, ra, vs, w, ctrl, part) : INT_MIN;
+      const int lb = hb ? cross_loc<COLW>(geo, g, qb, jb, rbw, vs, w, ctrl, part) : INT_MIN;
+      cross_apply<MODE, COLW>(la, ra, w, bm, rowslot, oddmax, side, ncross);
+      cross_apply<MODE, COLW>(lb, rbw, w, bm, rowslot, oddmax, side, ncross);
     }
   }
 }
@@ -233,11 +239,12 @@ __device__ __forceinline__ VtxState rotate_prev(const VtxState& s, VtxState& car
 // them into the window's bitmap.  Ring starts (no edge ends there) are the
 // part's first vertex and the ring ends of earlier rings; parts with at most
 // 32 rings keep those in registers.
-template <int MODE>
+template <int MODE, bool COLW>
 __device__ __forceinline__ void warp_pass(const Geo& geo, const Grid& g, unsigned long long rb,
                                           unsigned long long re, unsigned long long vs, unsigned vb, unsigned ve,
                                           const PolyWin& w, unsigned* bm, QEnt* q, const int* rowslot, int* oddmax,
-                                          Ctrl* ctrl, unsigned long long part, unsigned long long& ncross) {
+                                          unsigned* side, Ctrl* ctrl, unsigned long long part,
+                                          unsigned long long& ncross) {
   const int lane = threadIdx.x & 31;
   if (vb >= ve) return;
   const double2* xy = geo.xy + vs;
@@ -321,7 +328,7 @@ __device__ __forceinline__ void warp_pass(const Geo& geo, const Grid& g, unsigne
     nq += __popc(mask);
     if (nq > QCAP - 32 || base + 32 >= ve) {
       __syncwarp();
-      if (nq > 0) warp_cross<MODE>(geo, g, q, nq, vs, w, bm, rowslot, oddmax, ctrl, part, ncross);
+      if (nq > 0) warp_cross<MODE, COLW>(geo, g, q, nq, vs, w, bm, rowslot, oddmax, side, ctrl, part, ncross);
       nq = 0;
       __syncwarp();
     }
@@ -370,10 +377,12 @@ __device__ __forceinline__ void stage_flush(WarpScratch& ws, int& st_n, const Re
 // round; rows are contiguous runs of lanes, so the parity of the set bits
 // before each word comes from a row-segmented XOR scan plus the carry of the
 // previous round.
+// `side` (column windows, else nullptr): bit 0 of side[row] is the parity of
+// the row's crossings left of the window, which every word of the row takes.
 __device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw, int r0, int col0,
                                              const PartPlan& pl, unsigned part, WarpScratch& ws, int& st_n,
                                              const RecBuf& rb, unsigned* bucket_count, Ctrl* ctrl,
-                                             unsigned long long& npix) {
+                                             unsigned long long& npix, const unsigned* side) {
   const int lane = threadIdx.x & 31;
   const int nw = nr * bw;
   const float inv_bw = 1.0f / (float)bw;
@@ -406,6 +415,7 @@ __device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw,
       c_row = lrow;
       c_par = lpar;
     }
+    if (side && valid) before ^= side[row] & 1u;  // crossings left of a column window
     unsigned cov = bits;  // inclusive prefix XOR of the word's bits
     cov ^= cov << 1;
     cov ^= cov << 2;
@@ -429,17 +439,18 @@ __device__ __forceinline__ void warp_extract(const unsigned* bm, int nr, int bw,
   }
 }
 
-// rows of the window with an odd number of crossings (one lane per row)
+// rows of the window with an odd number of crossings (one lane per row);
+// a column window adds the crossings left and right of it (`side`)
 __device__ __forceinline__ void warp_find_odd_rows(const unsigned* bm, int rb, int re, int bw, int* rowslot,
-                                                   int* oddrow, int* oddmax, int* s_nodd) {
+                                                   int* oddrow, int* oddmax, int* s_nodd, const unsigned* side) {
   for (int i = rb + (threadIdx.x & 31); i < re; i += 32) {
-    unsigned par = 0;
+    unsigned par = side ? (side[i] ^ (side[i] >> 1)) : 0u;
     for (int wd = 0; wd < bw; ++wd) par ^= (unsigned)__popc(bm[i * bw + wd]);
     if (par & 1u) {
       const int slot = atomicAdd(s_nodd, 1);
       rowslot[i] = slot;
       oddrow[slot] = i;
-      oddmax[slot] = -1;
+      oddmax[slot] = INT_MIN;
     }
   }
 }
@@ -476,10 +487,12 @@ __device__ __forceinline__ void flush_counters(unsigned long long ncross, unsign
   }
 }
 
-__device__ __forceinline__ PolyWin make_window(const PartPlan& pl, int k) {
+// Row window k of a part whose columns fit one bitmap.
+__device__ __forceinline__ PolyWin make_row_window(const PartPlan& pl, int k) {
   PolyWin win;
   win.r0 = pl.row0 + k * pl.wr;
   win.r1 = min(win.r0 + pl.wr, pl.row1);
+  win.colwin = false;
   win.col0 = pl.col0;
   win.bw = pl.bw;
   win.nbits = pl.bw * 32;
@@ -488,8 +501,25 @@ __device__ __forceinline__ PolyWin make_window(const PartPlan& pl, int k) {
   return win;
 }
 
+// Window k of a part: row windows, or (parts wider than one bitmap) row
+// windows times column windows, column window fastest.
+__device__ __forceinline__ PolyWin make_window(const PartPlan& pl, unsigned long long k) {
+  PolyWin win;
+  const unsigned long long ncw = pl.ncw > 1 ? pl.ncw : 1;
+  const int kr = (int)(k / ncw), kc = (int)(k % ncw);
+  win.r0 = pl.row0 + kr * pl.wr;
+  win.r1 = min(win.r0 + pl.wr, pl.row1);
+  win.colwin = pl.ncw > 1;
+  win.col0 = pl.col0 + (win.colwin ? kc * COLWIN_WORDS * 32 : 0);
+  win.bw = win.colwin ? min(COLWIN_WORDS, pl.bw - kc * COLWIN_WORDS) : pl.bw;
+  win.nbits = win.bw * 32;
+  win.nrows = pl.nrows;
+  win.ncols = pl.ncols;
+  return win;
+}
+
 // ---- narrow parts: one window per warp ------------------------------------
-__global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo geo, Grid g,
+__global__ void __launch_bounds__(SMALL_WARPS * 32, 5) k_poly_spans_narrow(Geo geo, Grid g,
                                                                         const PartPlan* __restrict__ plan,
                                                                         const unsigned long long* __restrict__ poff,
                                                                         RecBuf sb, unsigned* bucket_count,
@@ -524,9 +554,9 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
       while (poff[(p + 1) * PC_N + PC_WIN_SMALL] <= wi) ++p;
     }
     const PartPlan pl = plan[p];
-    const int k = (int)(wi - poff[p * PC_N + PC_WIN_SMALL]);
-    const PolyWin win = make_window(pl, k);
-    const int nr = win.r1 - win.r0, bw = pl.bw;
+    const unsigned long long k = wi - poff[p * PC_N + PC_WIN_SMALL];
+    const PolyWin win = make_row_window(pl, (int)k);  // narrow parts never take column windows
+    const int nr = win.r1 - win.r0, bw = win.bw;
     for (int i = lane; i < nr * bw; i += 32) bm[i] = 0u;
     for (int i = lane; i < WR_MAX; i += 32) rowslot[i] = -1;
     if (lane == 0) *s_nodd = 0;
@@ -534,22 +564,22 @@ __global__ void __launch_bounds__(SMALL_WARPS * 32, 6) k_poly_spans_narrow(Geo g
     const unsigned long long vs = geo.vertex_offsets[rb];
     const unsigned nv = (unsigned)(geo.vertex_offsets[re] - vs);
     __syncwarp();
-    warp_pass<0>(geo, g, rb, re, vs, 0, nv, win, bm, ws.q, rowslot, oddmax, ctrl, p, ncross);
+    warp_pass<0, false>(geo, g, rb, re, vs, 0, nv, win, bm, ws.q, rowslot, oddmax, nullptr, ctrl, p, ncross);
     __syncwarp();
-    warp_find_odd_rows(bm, 0, nr, bw, rowslot, oddrow, oddmax, s_nodd);
+    warp_find_odd_rows(bm, 0, nr, bw, rowslot, oddrow, oddmax, s_nodd, nullptr);
     __syncwarp();
     const int nodd = *s_nodd;
     if (nodd > 0) {
       unsigned long long dummy = 0;
-      warp_pass<1>(geo, g, rb, re, vs, 0, nv, win, bm, ws.q, rowslot, oddmax, ctrl, p, dummy);
+      warp_pass<1, false>(geo, g, rb, re, vs, 0, nv, win, bm, ws.q, rowslot, oddmax, nullptr, ctrl, p, dummy);
       __syncwarp();
       for (int t = lane; t < nodd; t += 32) {
         const int i = oddrow[t], loc = oddmax[t];
-        if (loc >= 0) bm[i * bw + (loc >> 5)] ^= 1u << (loc & 31);
+        if (loc != INT_MIN) bm[i * bw + (loc >> 5)] ^= 1u << (loc & 31);
       }
       __syncwarp();
     }
-    warp_extract(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix);
+    warp_extract(bm, nr, bw, win.r0, win.col0, pl, (unsigned)p, ws, st_n, sb, bucket_count, ctrl, npix, nullptr);
     stage_flush(ws, st_n, sb, bucket_count, ctrl);  // the stage aliases the queue of the next window
     ++wi;
   }
@@ -572,6 +602,7 @@ __global__ void __launch_bounds__(POLY_THREADS) k_poly_spans(Geo geo, Grid g, co
   __shared__ int oddmax[WR_MAX];
   __shared__ int oddrow[WR_MAX];
   __shared__ int s_nodd;
+  __shared__ unsigned s_side[WR_MAX];  // column windows: parity of crossings left (bit 0) / right (bit 1)
   __shared__ unsigned long long s_part, s_w;
   if (ctrl->err) return;
   const unsigned long long total = poff[geo.n_parts * PC_N + PC_WINDOWS];
@@ -589,11 +620,15 @@ __global__ void __launch_bounds__(POLY_THREADS) k_poly_spans(Geo geo, Grid g, co
     __syncthreads();
     const unsigned long long p = s_part;
     const PartPlan pl = plan[p];
-    const int k = (int)(wi - poff[p * PC_N + PC_WINDOWS]);
+    const unsigned long long k = wi - poff[p * PC_N + PC_WINDOWS];
     const PolyWin win = make_window(pl, k);
-    const int nr = win.r1 - win.r0, bw = pl.bw;
+    const int nr = win.r1 - win.r0, bw = win.bw;
+    unsigned* side = win.colwin ? s_side : nullptr;
     for (int i = threadIdx.x; i < nr * bw; i += POLY_THREADS) bm[i] = 0u;
-    for (int i = threadIdx.x; i < WR_MAX; i += POLY_THREADS) rowslot[i] = -1;
+    for (int i = threadIdx.x; i < WR_MAX; i += POLY_THREADS) {
+      rowslot[i] = -1;
+      s_side[i] = 0u;
+    }
     if (threadIdx.x == 0) s_nodd = 0;
     const unsigned long long rb = geo.ring_offsets[p], re = geo.ring_offsets[p + 1];
     const unsigned long long vs = geo.vertex_offsets[rb];
@@ -601,24 +636,28 @@ __global__ void __launch_bounds__(POLY_THREADS) k_poly_spans(Geo geo, Grid g, co
     const unsigned vb = (unsigned)((unsigned long long)nv * warp / W);
     const unsigned ve = (unsigned)((unsigned long long)nv * (warp + 1) / W);
     __syncthreads();
-    warp_pass<0>(geo, g, rb, re, vs, vb, ve, win, bm, ws.q, rowslot, oddmax, ctrl, p, ncross);
+    warp_pass<0, true>(geo, g, rb, re, vs, vb, ve, win, bm, ws.q, rowslot, oddmax, side, ctrl, p, ncross);
     __syncthreads();
     const int rlo = nr * warp / W, rhi = nr * (warp + 1) / W;
-    warp_find_odd_rows(bm, rlo, rhi, bw, rowslot, oddrow, oddmax, &s_nodd);
+    warp_find_odd_rows(bm, rlo, rhi, bw, rowslot, oddrow, oddmax, &s_nodd, side);
     __syncthreads();
     const int nodd = s_nodd;
     if (nodd > 0) {
       unsigned long long dummy = 0;
-      warp_pass<1>(geo, g, rb, re, vs, vb, ve, win, bm, ws.q, rowslot, oddmax, ctrl, p, dummy);
+      warp_pass<1, true>(geo, g, rb, re, vs, vb, ve, win, bm, ws.q, rowslot, oddmax, side, ctrl, p, dummy);
       __syncthreads();
+      // drop the largest crossing of each odd row again: in the bitmap, or in
+      // the carry when it lies left of a column window (right of it: no effect)
       for (int t = threadIdx.x; t < nodd; t += POLY_THREADS) {
         const int i = oddrow[t], loc = oddmax[t];
-        if (loc >= 0) bm[i * bw + (loc >> 5)] ^= 1u << (loc & 31);
+        if (loc == INT_MIN) continue;
+        if (loc < 0) s_side[i] ^= 1u;
+        else if (loc < win.nbits) bm[i * bw + (loc >> 5)] ^= 1u << (loc & 31);
       }
       __syncthreads();
     }
     warp_extract(bm + rlo * bw, rhi - rlo, bw, win.r0 + rlo, win.col0, pl, (unsigned)p, ws, st_n, sb,
-                 bucket_count, ctrl, npix);
+                 bucket_count, ctrl, npix, side ? side + rlo : nullptr);
     stage_flush(ws, st_n, sb, bucket_count, ctrl);
     __syncthreads();
   }

@@ -164,6 +164,8 @@ class BurnServer:
         self._stats_lock = threading.Lock()
         self.batches = 0
         self.jobs_done = 0
+        self.device_ms = 0.0  # engine-measured device time of every batch call, summed over streams
+        self.call_ms = 0.0    # host time inside the batch calls (allocation + call), summed
         self._contexts = [_lib.Context(device) for _ in range(max(1, streams))]
         self._threads = [threading.Thread(target=self._run, args=(c,), daemon=True) for c in self._contexts]
         for t in self._threads:
@@ -222,8 +224,9 @@ class BurnServer:
             try:
                 outs = [torch.empty(max(1, r.nbytes), dtype=torch.uint8, device=dev) for r in batch]
                 torch.cuda.current_stream(dev).synchronize()  # allocations ordered before the engine stream
+                st: dict = {}
                 rasterize_batch_device([r.job for r in batch], dtype=batch[0].dtype, outs=outs, context=ctx,
-                                       wave_bytes=self.wave_bytes)
+                                       wave_bytes=self.wave_bytes, stats=st)
             except Exception as e:  # every request of the batch sees the error; later batches go on
                 outs = None
                 for r in batch:
@@ -234,6 +237,8 @@ class BurnServer:
             with self._stats_lock:
                 self.batches += 1
                 self.jobs_done += len(batch)
+                self.device_ms += float(st.get("ms_device_total", 0.0))
+                self.call_ms += (t1 - t0) * 1e3
             results = [Result(o, r.t_submit, t0, t1, len(batch), self, r.nbytes) for r, o in zip(batch, outs)]
             del outs  # the results own the rasters now: a release frees them
             for r, res in zip(batch, results):

@@ -94,3 +94,45 @@ def test_more_than_2_28_buckets_in_passes_against_oracle():
     ref = oracle_burn(t, info, fn="sum", values=vals, background=0, dtype="uint8", bands=bands, n_bands=16)
     assert same_bits(got, ref), diff_report(got, ref)
     assert int(ref.astype(np.uint64).sum()) > 0
+
+
+def test_polygons_wider_than_one_bitmap_against_oracle():
+    """Parts wider than the 8,192-word (262,144-pixel) bitmap burn in column
+    windows: crossings left of a window flip its rows' parity, the largest
+    crossing of an odd row is dropped wherever it lies.  A 400,000-column
+    raster, 300 rows: long thin polygons, a huge star polygon (most of whose
+    edges miss the rows) with a hole, and small ones on top, checked with
+    `sum` (order) and `count` against the oracle."""
+    rng = np.random.default_rng(21)
+    ncols, nrows = 400_000, 300
+    b = G.TableBuilder()
+    # a band across the whole width with a notch, and a sliver
+    G.add_polygon(b, [(-10.0, 20.5), (400_010.0, 35.2), (399_000.0, 120.0), (200_000.0, 90.0), (-5.0, 140.0)])
+    G.add_polygon(b, [(1000.5, 200.0), (350_000.25, 205.0), (1000.5, 210.0)])
+    # a star polygon of radius ~190k centred on the raster, with a hole
+    n = 300
+    ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+    rad = 190_000.0 * rng.uniform(0.4, 1.0, n)
+    ext = np.stack([200_000.0 + rad * np.cos(ang), 150.0 + rad * np.sin(ang) * 0.001], axis=1)
+    hole = np.array([[150_000.0, 140.0], [250_000.0, 145.0], [240_000.0, 160.0], [160_000.0, 158.0]])
+    G.add_polygon(b, ext, [hole])
+    for _ in range(200):  # small polygons everywhere
+        cx, cy = rng.uniform(0, ncols), rng.uniform(0, nrows)
+        k = int(rng.integers(5, 30))
+        a = np.sort(rng.uniform(0, 2 * np.pi, k))
+        r = rng.uniform(2, 40, k)
+        G.add_polygon(b, np.stack([cx + r * np.cos(a), cy + r * np.sin(a)], axis=1))
+    t = b.build()
+    info = rz.RasterInfo(nrows, ncols, 0.0, float(ncols), 0.0, float(nrows), 1.0, 1.0)
+    vals = (np.arange(t.n_geoms) % 17 + 1).astype(np.float64)
+    for fn, dt, bg in (("sum", "float64", np.nan), ("count", "uint32", 0)):
+        v = vals if fn == "sum" else None
+        got = gpu_burn(t, info, fn=fn, values=v, background=bg, dtype=dt)
+        ref = oracle_burn(t, info, fn=fn, values=v, background=bg, dtype=dt)
+        assert same_bits(got, ref), f"{fn}: " + diff_report(got, ref)
+    # the windows also hold with a row window and all_touched
+    got = rz.rasterize_table(t, info, fn="count", background=0, dtype="uint32", rows=(100, 180))
+    assert same_bits(got, ref[:, 100:180])
+    got = gpu_burn(t, info, fn="max", values=vals, background=0.0, dtype="float64", all_touched=True)
+    ref = oracle_burn(t, info, fn="max", values=vals, background=0.0, dtype="float64", all_touched=True)
+    assert same_bits(got, ref), "all_touched: " + diff_report(got, ref)
