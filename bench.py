@@ -638,11 +638,11 @@ def main():
     ap.add_argument("--batch-legs", default="plain,batched", help="legs of the batched comparison to run")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="arrival window per rate (0: skip)")
     ap.add_argument("--serve-rates", default="200,1000,5000")
-    ap.add_argument("--serve-plain-max-rate", type=float, default=1000.0)
+    ap.add_argument("--serve-plain-max-rate", type=float, default=5000.0)
     ap.add_argument("--serve-pool", type=int, default=96)
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)
     ap.add_argument("--serve-max-batch", type=int, default=512)
-    ap.add_argument("--serve-drain-limit", type=float, default=60.0,
+    ap.add_argument("--serve-drain-limit", type=float, default=10.0,
                     help="seconds to wait for the backlog after the arrival window before cancelling it")
     args = ap.parse_args()
     if args.impl == "reference":
