@@ -108,18 +108,19 @@ class Admission:
                     return []
                 self._cv.wait(left)
             dtype = self._pending[0].dtype
-            batch, keep = [], collections.deque()
+            # cost proportional to the requests looked at, not to the backlog: the skipped ones
+            # go back to the front of the queue in their order
+            batch, skipped = [], []
             while self._pending and len(batch) < self.max_batch:
                 r = self._pending.popleft()
                 if r.dtype == dtype and self.reserved + r.nbytes <= self.budget:
                     self.reserved += r.nbytes
                     batch.append(r)
                 else:
-                    keep.append(r)
+                    skipped.append(r)
                     if r.dtype == dtype:  # arrival order within a dtype: nothing overtakes it
                         break
-            keep.extend(self._pending)
-            self._pending = keep
+            self._pending.extendleft(reversed(skipped))
             self.peak_reserved = max(self.peak_reserved, self.reserved)
             return batch
 

@@ -72,6 +72,32 @@ def test_admission_batch_cap_and_blocking_take():
     assert got == [[r]]
 
 
+def test_admission_take_costs_the_requests_it_looks_at_not_the_backlog():
+    """A server that has fallen behind holds a backlog of hundreds of thousands
+    of requests; one take at one request per batch must not copy it.  20,000
+    takes from a 200,000-request backlog finish in well under the time one
+    copy of the backlog per take would need (4e9 element moves), and the
+    skipped requests of the other dtype keep their place at the front."""
+    a = Admission(budget_bytes=1 << 40, max_batch=1)
+    reqs = [_req(1, "uint8" if i % 2 else "float32") for i in range(200_000)]
+    for r in reqs:
+        a.put(r)
+    t0 = time.perf_counter()
+    out = []
+    for _ in range(20_000):
+        out.extend(a.take(timeout=0))
+    assert time.perf_counter() - t0 < 5.0
+    assert out == reqs[:20_000]  # alternating dtypes: the head is always the oldest request
+    assert len(a) == 180_000
+    a2 = Admission(budget_bytes=1 << 40, max_batch=2)
+    rs = [_req(1), _req(1, "uint8"), _req(1, "uint8"), _req(1), _req(1, "uint8")]
+    for r in rs:
+        a2.put(r)
+    assert a2.take(timeout=0) == [rs[0], rs[3]]
+    assert a2.take(timeout=0) == [rs[1], rs[2]]
+    assert a2.take(timeout=0) == [rs[4]]
+
+
 # ---------------------------------------------------------------- GPU ------
 @pytest.mark.gpu
 def test_server_results_equal_single_burns_and_batches_form():
