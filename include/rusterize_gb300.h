@@ -266,6 +266,22 @@ rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, const void* va
 rz_status rz_sparse_view_get(const rz_sparse* sp, rz_sparse_view* out);
 void rz_sparse_free(rz_sparse* sp);
 
+/* Replaces SparseArray::build_array (rust/src/encoding/arrays.rs:103-141):
+ * replays a COO triplet stream onto a raster of n_bands x nrows x ncols
+ * values of `dtype` (C order) that starts at `background` (one host value),
+ * applying `fn` to each pixel's writes in stream order.  The stream is laid
+ * out as in rz_sparse_view: band_counts[b] triplets for band b, bands in
+ * order.  band_counts is a host array; rows, cols (uint64) and values (of
+ * `dtype`) are host arrays, or device arrays with RZ_FLAG_INPUT_DEVICE; out is
+ * host memory, or device memory with RZ_FLAG_OUTPUT_DEVICE.  A triplet
+ * outside the raster gives RZ_VALUE_ERROR (the reference's indexing panics);
+ * the output is then unspecified.  `stats` may be NULL: ms_fill is the
+ * replay's device time, pixel_writes the number of triplets. */
+rz_status rz_sparse_build(rz_context* ctx, const uint64_t* band_counts, uint32_t n_bands, const uint64_t* rows,
+                          const uint64_t* cols, const void* values, uint64_t nrows, uint64_t ncols, rz_pixel_fn fn,
+                          rz_dtype dtype, const void* background, uint32_t flags, void* out, rz_stats* stats,
+                          char* err, size_t errlen);
+
 /* ---- batches of independent jobs ---------------------------------------- */
 
 /* One job of a batch: the arguments of one single-band rz_rasterize call. */

@@ -54,6 +54,9 @@ def load():
                                              c_int, c_void_p, c_uint32, c_void_p, c_uint64, c_uint64, c_int, c_int,
                                              POINTER(c_uint64), POINTER(c_void_p), POINTER(c_void_p),
                                              POINTER(c_void_p), c_void_p]
+        lib.rzo_sparse_build.restype = c_int
+        lib.rzo_sparse_build.argtypes = [c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_int, c_uint64, c_uint64,
+                                         c_int, c_void_p, c_void_p]
         lib.rzo_free.restype = None
         lib.rzo_free.argtypes = [c_void_p]
         _lib = lib
@@ -165,3 +168,23 @@ def rasterize_sparse(table, nrows, ncols, xmin, xmax, ymin, ymax, xres, yres, *,
             lib.rzo_free(p_)
     return band_counts, rows, cols, out_vals
 
+
+def sparse_build(band_counts, rows, cols, values, nrows, ncols, *, fn="last", background=0):
+    """SparseArray::build_array with the CPU restatement: the triplet stream
+    (band_counts[b] triplets for band b, bands in order) replayed onto a
+    (bands, nrows, ncols) background raster of the values' dtype."""
+    lib = load()
+    counts = np.ascontiguousarray(band_counts, np.uint64)
+    rows = np.ascontiguousarray(rows, np.uint64)
+    cols = np.ascontiguousarray(cols, np.uint64)
+    vals = np.ascontiguousarray(values)
+    dt = vals.dtype
+    out = np.empty((len(counts), int(nrows), int(ncols)), dtype=dt)
+    bg = np.array([background], dtype=dt)
+    st = lib.rzo_sparse_build(counts.ctypes.data, len(counts), rows.ctypes.data, cols.ctypes.data, vals.ctypes.data,
+                              DTYPES[dt.name], nrows, ncols, PIXEL_FNS[fn], bg.ctypes.data, out.ctypes.data)
+    if st == -3:
+        raise ValueError("triplet outside the raster")
+    if st:
+        raise ValueError(f"oracle failed with status {st}")
+    return out

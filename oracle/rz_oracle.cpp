@@ -545,6 +545,27 @@ void bbox_add_point(BBox& b, double x, double y) {
   if (y > b.ymax) b.ymax = y; else if (y < b.ymin) b.ymin = y;
 }
 
+// SparseArray::build_array (rust/src/encoding/arrays.rs:103-141): the raster
+// starts at the background, and each band's triplets, in order, apply the
+// pixel function to their pixel.  -3 for a triplet outside the raster, where
+// the reference's array indexing panics.
+template <typename T>
+int sparse_build_t(const uint64_t* band_counts, uint32_t n_bands, const uint64_t* rows, const uint64_t* cols,
+                   const T* vals, uint64_t nrows, uint64_t ncols, int fn, T bg, T* out) {
+  const uint64_t plane = nrows * ncols;
+  std::fill(out, out + (uint64_t)n_bands * plane, bg);
+  uint64_t off = 0;
+  for (uint32_t b = 0; b < n_bands; ++b) {
+    T* band = out + (uint64_t)b * plane;
+    for (uint64_t i = off; i < off + band_counts[b]; ++i) {
+      if (rows[i] >= nrows || cols[i] >= ncols) return -3;
+      apply_fn(fn, band[rows[i] * ncols + cols[i]], vals[i], bg);
+    }
+    off += band_counts[b];
+  }
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -715,6 +736,31 @@ int rzo_raster_info(uint64_t n_geoms, const uint64_t* part_offsets, const uint8_
   out_info[4] = xres; out_info[5] = yres;
   out_shape[0] = nrows; out_shape[1] = ncols;
   return 0;
+}
+
+// Replay of a triplet stream onto a background raster (n_bands x nrows x
+// ncols of `dtype`); bg points at one value of `dtype`.
+int rzo_sparse_build(const uint64_t* band_counts, uint32_t n_bands, const uint64_t* rows, const uint64_t* cols,
+                     const void* vals, int dtype, uint64_t nrows, uint64_t ncols, int pixel_fn, const void* bg,
+                     void* out) {
+#define RZO_BCASE(CODE, T)                                                                              \
+  case CODE:                                                                                           \
+    return sparse_build_t<T>(band_counts, n_bands, rows, cols, (const T*)vals, nrows, ncols, pixel_fn, \
+                             *(const T*)bg, (T*)out);
+  switch (dtype) {
+    RZO_BCASE(DT_U8, uint8_t)
+    RZO_BCASE(DT_U16, uint16_t)
+    RZO_BCASE(DT_U32, uint32_t)
+    RZO_BCASE(DT_U64, uint64_t)
+    RZO_BCASE(DT_I8, int8_t)
+    RZO_BCASE(DT_I16, int16_t)
+    RZO_BCASE(DT_I32, int32_t)
+    RZO_BCASE(DT_I64, int64_t)
+    RZO_BCASE(DT_F32, float)
+    RZO_BCASE(DT_F64, double)
+    default: return -2;
+  }
+#undef RZO_BCASE
 }
 
 }  // extern "C"

@@ -159,6 +159,8 @@ PROTOTYPES = {
                                     c_int, c_int, c_uint32, POINTER(c_void_p), POINTER(RzStats), c_char_p, c_size_t]),
     "rz_sparse_view_get": (c_int, [c_void_p, POINTER(RzSparseView)]),
     "rz_sparse_free": (None, [c_void_p]),
+    "rz_sparse_build": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_void_p, c_void_p, c_uint64, c_uint64,
+                                c_int, c_int, c_void_p, c_uint32, c_void_p, POINTER(RzStats), c_char_p, c_size_t]),
     "rz_rasterize_batch": (c_int, [c_void_p, POINTER(RzJob), c_size_t, c_int, c_uint32, c_uint64,
                                    POINTER(RzBatchStats), c_char_p, c_size_t]),
 }

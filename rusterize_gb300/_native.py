@@ -19,7 +19,7 @@ from ._dependencies import shapely
 from ._lib import PanicException
 from .engine import RasterInfo, raster_info, rasterize_table, rasterize_table_sparse
 from .geometry import GeometryTable, from_wkb, from_wkt
-from .sparse import SparseArray, _Burn
+from .sparse import SparseArray
 
 
 def parse_geometry(obj: Any) -> GeometryTable:
@@ -177,9 +177,7 @@ def _rusterize(geometry: Any, raw_raster_info: dict, pypixel_fn: str, pydf: Any 
         band_counts, rows, cols, vals = rasterize_table_sparse(
             table, info, values=values, fn=pypixel_fn, dtype=pydtype, bands=bands, n_bands=len(band_names),
             all_touched=bool(pytouched), context=context, stats=stats)
-        burn = _Burn(table=table, values=values, fn=pypixel_fn, dtype=pydtype, background=bg, bands=bands,
-                     all_touched=bool(pytouched))
-        return SparseArray(band_names, band_counts, rows, cols, vals, info, burn)
+        return SparseArray(band_names, band_counts, rows, cols, vals, info, pypixel_fn, bg)
     out = rasterize_table(table, info, values=values, fn=pypixel_fn, background=bg, dtype=pydtype, bands=bands,
                           n_bands=len(band_names), all_touched=bool(pytouched), context=context, stats=stats)
     if pyencoding == "xarray":

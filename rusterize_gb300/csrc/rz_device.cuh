@@ -82,6 +82,7 @@ enum : unsigned {
   ERR_LINE_LONG = 6,   // segment needs more than LINE_MAX_STEPS steps
   ERR_BAD_JOB = 7,     // a batch job's table does not start at 0 / end at its counts
   ERR_RANGE = 8,       // a record or a raster tile outside the call's buckets (an engine defect)
+  ERR_TRIPLET = 9,     // a sparse triplet outside the raster it is replayed onto
 };
 
 // Device control block, reset at the start of every pass.

@@ -22,6 +22,7 @@
 #include "rz_kernels.cuh"
 #include "rz_scan.cuh"
 #include "rz_sort.cuh"
+#include "rz_replay.cuh"
 #include "rz_sparse.cuh"
 
 using rz::fail;
@@ -146,6 +147,8 @@ rz_status ctrl_error(const Ctrl& hc, char* err, size_t errlen) {
     case ERR_RANGE:
       return fail(err, errlen, RZ_RUNTIME_ERROR, "internal error: record or tile outside the call's rasters (%llu)",
                   ix);
+    case ERR_TRIPLET:
+      return fail(err, errlen, RZ_VALUE_ERROR, "triplet %llu lies outside the raster", ix);
     case ERR_BAD_JOB:
       return fail(err, errlen, RZ_INVALID_ARGUMENT,
                   "geometry table of job %llu does not start at 0 or end at its own counts", ix);
@@ -1052,6 +1055,189 @@ extern "C" rz_status rz_sparse_view_get(const rz_sparse* sp, rz_sparse_view* out
 }
 
 extern "C" void rz_sparse_free(rz_sparse* sp) { delete sp; }
+
+// ---------------------------------------------------------------------------
+// Replay of a triplet stream onto a raster (SparseArray::build_array,
+// rust/src/encoding/arrays.rs:103-141): chunks of the stream in order, each
+// keyed by pixel, stably sorted and folded (rz_replay.cuh).
+
+namespace {
+
+typedef int (*replay_fn)(const ReplayArgs&, int, int, cudaStream_t);
+
+replay_fn replay_for(rz_dtype dt) {
+  switch (dt) {
+    case RZ_U8: return rz_replay_u8;
+    case RZ_U16: return rz_replay_u16;
+    case RZ_U32: return rz_replay_u32;
+    case RZ_U64: return rz_replay_u64;
+    case RZ_I8: return rz_replay_i8;
+    case RZ_I16: return rz_replay_i16;
+    case RZ_I32: return rz_replay_i32;
+    case RZ_I64: return rz_replay_i64;
+    case RZ_F32: return rz_replay_f32;
+    case RZ_F64: return rz_replay_f64;
+  }
+  return nullptr;
+}
+
+// triplets keyed, sorted and folded at once (56 B of scratch each)
+constexpr unsigned long long kReplayChunk = 1ull << 28;
+
+}  // namespace
+
+static rz_status replay_impl(rz_context* ctx, const uint64_t* band_counts, uint32_t n_bands, const uint64_t* rows,
+                             const uint64_t* cols, const void* values, uint64_t nrows, uint64_t ncols,
+                             rz_pixel_fn fn, rz_dtype dt, const void* background, uint32_t flags, void* out,
+                             rz_stats* stats, char* err, size_t errlen) {
+  using clk = std::chrono::steady_clock;
+  const auto t_host0 = clk::now();
+  rz::clear_err(err, errlen);
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (!ctx || !band_counts || !background || !out) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null argument");
+  const size_t tsize = rz_dtype_size(dt);
+  if (tsize == 0) return fail(err, errlen, RZ_VALUE_ERROR, "Unsupported dtype");
+  if ((int)fn < 0 || (int)fn > 6) return fail(err, errlen, RZ_VALUE_ERROR, "Unknown pixel function");
+  if (n_bands == 0) return fail(err, errlen, RZ_INVALID_ARGUMENT, "n_bands must be > 0");
+  const bool in_dev = flags & RZ_FLAG_INPUT_DEVICE, out_dev = flags & RZ_FLAG_OUTPUT_DEVICE;
+  const bool timing = !(flags & RZ_FLAG_NO_TIMING);
+  std::vector<unsigned long long> bstart(n_bands + 1ull, 0ull);
+  for (uint32_t b = 0; b < n_bands; ++b) {
+    bstart[b + 1] = bstart[b] + band_counts[b];
+    if (bstart[b + 1] < bstart[b]) return fail(err, errlen, RZ_VALUE_ERROR, "band counts overflow");
+  }
+  const unsigned long long count = bstart[n_bands];
+  if (count && (!rows || !cols || !values)) return fail(err, errlen, RZ_INVALID_ARGUMENT, "null triplet arrays");
+  if (in_dev && count &&
+      ((reinterpret_cast<uintptr_t>(rows) | reinterpret_cast<uintptr_t>(cols)) & 7 ||
+       reinterpret_cast<uintptr_t>(values) % tsize))
+    return fail(err, errlen, RZ_INVALID_ARGUMENT, "device triplet arrays must be aligned to their element size");
+  // raster elements, with the product checked against 64 bits
+  unsigned long long px = n_bands;
+  for (unsigned long long d : {(unsigned long long)nrows, (unsigned long long)ncols}) {
+    if (d && px > ~0ull / d) return fail(err, errlen, RZ_VALUE_ERROR, "raster too large");
+    px *= d;
+  }
+  if (px > (~0ull >> 4) / tsize) return fail(err, errlen, RZ_VALUE_ERROR, "raster too large");
+  if (stats) {
+    stats->out_bytes = px * tsize;
+    stats->pixel_writes = count;
+  }
+  if (px == 0) {
+    if (count) return fail(err, errlen, RZ_VALUE_ERROR, "triplet 0 lies outside the raster");
+    return RZ_OK;
+  }
+
+  RZ_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const int sms = ctx->num_sms;
+  const unsigned long long chunk = std::max(1ull, std::min(count, kReplayChunk));
+  Layout L;
+  const size_t o_ctrl = L.take(sizeof(Ctrl));
+  const size_t o_bs = L.take(8 * (n_bands + 1ull));
+  size_t o_rows = 0, o_cols = 0, o_vals = 0;
+  if (!in_dev) {
+    o_rows = L.take(8 * chunk);
+    o_cols = L.take(8 * chunk);
+    o_vals = L.take(tsize * chunk);
+  }
+  const size_t o_k0 = L.take(8 * chunk), o_k1 = L.take(8 * chunk);
+  const size_t o_v0 = L.take(4 * chunk), o_v1 = L.take(4 * chunk);
+  const size_t o_rst = L.take(4 * radix_sort_temp_words(chunk));
+  RZ_CUDA(ensure(ctx->sparse, L.off));
+  void* d_ras = out;
+  if (!out_dev) {
+    RZ_CUDA(ensure(ctx->out, px * tsize));
+    d_ras = ctx->out.p;
+  }
+  char* base = static_cast<char*>(ctx->sparse.p);
+  auto at = [&](size_t o) { return static_cast<void*>(base + o); };
+  Ctrl* d_ctrl = static_cast<Ctrl*>(at(o_ctrl));
+  unsigned long long* d_bs = static_cast<unsigned long long*>(at(o_bs));
+  unsigned long long* k0 = static_cast<unsigned long long*>(at(o_k0));
+  unsigned long long* k1 = static_cast<unsigned long long*>(at(o_k1));
+  unsigned* v0 = static_cast<unsigned*>(at(o_v0));
+  unsigned* v1 = static_cast<unsigned*>(at(o_v1));
+  unsigned long long bg_bits = 0;
+  std::memcpy(&bg_bits, background, tsize);
+  int launches = 0;
+
+  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[0], s));
+  RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
+  RZ_CUDA(cudaMemcpyAsync(d_bs, bstart.data(), 8 * (n_bands + 1ull), cudaMemcpyHostToDevice, s));
+  {
+    const unsigned g = grid_for(px, 256, sms * 16);
+    switch (tsize) {
+      case 1: k_replay_bg<1><<<g, 256, 0, s>>>(d_ras, px, bg_bits); break;
+      case 2: k_replay_bg<2><<<g, 256, 0, s>>>(d_ras, px, bg_bits); break;
+      case 4: k_replay_bg<4><<<g, 256, 0, s>>>(d_ras, px, bg_bits); break;
+      default: k_replay_bg<8><<<g, 256, 0, s>>>(d_ras, px, bg_bits); break;
+    }
+    ++launches;
+  }
+  int bits = 1;  // keys are < px
+  while (bits < 64 && (1ull << bits) < px) ++bits;
+  const replay_fn rf = replay_for(dt);
+  for (unsigned long long t0 = 0; t0 < count; t0 += chunk) {
+    const unsigned m = (unsigned)std::min(chunk, count - t0);
+    const unsigned long long* drows;
+    const unsigned long long* dcols;
+    const void* dvals;
+    if (in_dev) {
+      drows = reinterpret_cast<const unsigned long long*>(rows) + t0;
+      dcols = reinterpret_cast<const unsigned long long*>(cols) + t0;
+      dvals = static_cast<const char*>(values) + tsize * t0;
+    } else {
+      // the previous chunk's kernels read these buffers earlier in stream order
+      RZ_CUDA(cudaMemcpyAsync(at(o_rows), rows + t0, 8ull * m, cudaMemcpyHostToDevice, s));
+      RZ_CUDA(cudaMemcpyAsync(at(o_cols), cols + t0, 8ull * m, cudaMemcpyHostToDevice, s));
+      RZ_CUDA(cudaMemcpyAsync(at(o_vals), static_cast<const char*>(values) + tsize * t0, tsize * m,
+                              cudaMemcpyHostToDevice, s));
+      drows = static_cast<const unsigned long long*>(at(o_rows));
+      dcols = static_cast<const unsigned long long*>(at(o_cols));
+      dvals = at(o_vals);
+    }
+    k_replay_keys<<<grid_for(m, 256, sms * 16), 256, 0, s>>>(drows, dcols, m, t0, d_bs, n_bands, nrows, ncols, k0,
+                                                              v0, d_ctrl);
+    ++launches;
+    const bool in_tmp = radix_sort(k0, v0, k1, v1, m, bits, static_cast<unsigned*>(at(o_rst)), s, launches);
+    ReplayArgs ra;
+    ra.skeys = in_tmp ? k1 : k0;
+    ra.sidx = in_tmp ? v1 : v0;
+    ra.n = m;
+    ra.vals = dvals;
+    ra.raster = d_ras;
+    ra.bg = bg_bits;
+    launches += rf(ra, (int)fn, sms, s);
+    RZ_CUDA(cudaGetLastError());
+  }
+  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[5], s));
+  RZ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+  RZ_CUDA(cudaStreamSynchronize(s));
+  if (ctx->h_ctrl->err) return ctrl_error(*ctx->h_ctrl, err, errlen);
+  if (!out_dev) RZ_CUDA(cudaMemcpyAsync(out, d_ras, px * tsize, cudaMemcpyDeviceToHost, s));
+  if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[6], s));
+  RZ_CUDA(cudaStreamSynchronize(s));
+  if (stats) {
+    stats->kernel_launches = (uint32_t)launches;
+    if (timing) {
+      cudaEventElapsedTime(&stats->ms_fill, ctx->ev[0], ctx->ev[5]);
+      cudaEventElapsedTime(&stats->ms_d2h, ctx->ev[5], ctx->ev[6]);
+      cudaEventElapsedTime(&stats->ms_device_total, ctx->ev[0], ctx->ev[6]);
+    }
+    stats->ms_host_total = std::chrono::duration<float, std::milli>(clk::now() - t_host0).count();
+  }
+  return RZ_OK;
+}
+
+extern "C" rz_status rz_sparse_build(rz_context* ctx, const uint64_t* band_counts, uint32_t n_bands,
+                                     const uint64_t* rows, const uint64_t* cols, const void* values, uint64_t nrows,
+                                     uint64_t ncols, rz_pixel_fn fn, rz_dtype dt, const void* background,
+                                     uint32_t flags, void* out, rz_stats* stats, char* err, size_t errlen) {
+  return drain_on_error(ctx ? ctx->stream : nullptr,
+                        replay_impl(ctx, band_counts, n_bands, rows, cols, values, nrows, ncols, fn, dt, background,
+                                    flags, out, stats, err, errlen));
+}
 
 // ---------------------------------------------------------------------------
 // Allocation-free burn (rz_rasterize_noalloc).

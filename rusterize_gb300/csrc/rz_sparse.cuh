@@ -88,4 +88,43 @@ __global__ void k_sparse_emit(const unsigned long long* __restrict__ skeys, cons
   }
 }
 
+// ---- replay of a triplet stream (SparseArray::build_array) ----
+
+// Key of every triplet of a chunk: the band comes from the band start
+// offsets (bstart[b] <= t < bstart[b + 1] for stream index t), rows and
+// columns are checked against the raster (the reference indexes the array and
+// panics outside it; here the first bad stream index is reported).
+__global__ void k_replay_keys(const unsigned long long* __restrict__ rows, const unsigned long long* __restrict__ cols,
+                              unsigned n, unsigned long long t0, const unsigned long long* __restrict__ bstart,
+                              unsigned n_bands, unsigned long long nrows, unsigned long long ncols,
+                              unsigned long long* keys, unsigned* idx, Ctrl* ctrl) {
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long t = t0 + i;
+    unsigned lo = 0, hi = n_bands - 1;  // the last band whose start is <= t
+    while (lo < hi) {
+      const unsigned mid = lo + (hi - lo + 1) / 2;
+      if (bstart[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const unsigned long long r = rows[i], c = cols[i];
+    unsigned long long key = 0;
+    if (r < nrows && c < ncols) key = ((unsigned long long)lo * nrows + r) * ncols + c;
+    else set_error(ctrl, ERR_TRIPLET, t);
+    keys[i] = key;
+    idx[i] = i;
+  }
+}
+
+// Background of a raster of n elements of VB bytes.
+template <int VB>
+__global__ void k_replay_bg(void* p, unsigned long long n, unsigned long long bg) {
+  using U = typename std::conditional<VB == 1, unsigned char,
+            typename std::conditional<VB == 2, unsigned short,
+            typename std::conditional<VB == 4, unsigned, unsigned long long>::type>::type>::type;
+  U* q = static_cast<U*>(p);
+  const U v = (U)bg;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    q[i] = v;
+}
+
 }  // namespace rzd

@@ -200,6 +200,49 @@ def rasterize_table_sparse(table: GeometryTable, info: RasterInfo, *, values=Non
     return band_counts, rows, cols, vals
 
 
+def sparse_build(band_counts, rows, cols, values, nrows: int, ncols: int, *, fn: str, background,
+                 context: _lib.Context | None = None, out: np.ndarray | None = None,
+                 stats: dict | None = None) -> np.ndarray:
+    """Replay a COO triplet stream onto a (bands, nrows, ncols) raster of the
+    values' dtype (``rz_sparse_build``; SparseArray::build_array,
+    rust/src/encoding/arrays.rs:103-141): the raster starts at
+    ``background`` and every triplet applies the pixel function ``fn`` to its
+    pixel, each pixel's writes in stream order.  band_counts[b] triplets
+    belong to band b, bands in order."""
+    lib = _lib.load()
+    if fn not in _lib.PIXEL_FNS:
+        raise ValueError("Unknown pixel function")
+    values = np.ascontiguousarray(values)
+    dtype = values.dtype.name
+    if dtype not in _lib.DTYPES:
+        raise ValueError(f"Unsupported dtype {dtype!r}")
+    counts = np.ascontiguousarray(band_counts, dtype=np.uint64)
+    if counts.ndim != 1 or len(counts) == 0:
+        raise ValueError("band_counts needs one count per band")
+    rows = np.ascontiguousarray(rows, dtype=np.uint64)
+    cols = np.ascontiguousarray(cols, dtype=np.uint64)
+    n = int(counts.sum(dtype=np.uint64))
+    if not len(rows) == len(cols) == len(values) == n:
+        raise ValueError("rows, cols, values and the band counts disagree")
+    shape = (len(counts), int(nrows), int(ncols))
+    if out is None:
+        out = np.empty(shape, dtype=values.dtype)
+    elif out.dtype != values.dtype or out.shape != shape or not out.flags.c_contiguous:
+        raise ValueError("out has the wrong dtype, shape or layout")
+    bg = np.array([background], dtype=values.dtype)
+    ctx = context or _lib.default_context()
+    st_c = _lib.RzStats()
+    e = _lib.errbuf()
+    with ctx.lock:
+        st = lib.rz_sparse_build(ctx.handle, counts.ctypes.data, len(counts), rows.ctypes.data, cols.ctypes.data,
+                                 values.ctypes.data, shape[1], shape[2], _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype],
+                                 bg.ctypes.data, 0, out.ctypes.data, ctypes.byref(st_c), e, len(e))
+    _lib.raise_for(st, e.value)
+    if stats is not None:
+        stats.update(st_c.as_dict())
+    return out
+
+
 
 @dataclass
 class BatchJob:

@@ -6,46 +6,36 @@ The triplets come from the GPU engine (``rz_rasterize_sparse``): one
 (row, col, value) triplet per pixel write, grouped by band in band order and
 within a band by geometry in input order -- the reference's stream, except
 that the triplets of one geometry come row by row, left to right.  Every
-pixel therefore sees the same sequence of writes, and ``to_numpy`` (the
-reference's ``build_array``: the writes replayed onto a background raster
-with the pixel function) equals the dense encoding bit for bit; it is
-materialised by the same engine.
+pixel therefore sees the same sequence of writes.  ``to_numpy`` is the
+reference's ``build_array``: the stored triplets replayed onto a background
+raster with the pixel function, on the GPU (``rz_sparse_build``), which
+equals the dense encoding of the same burn bit for bit.
 """
 
 from __future__ import annotations
-
-from dataclasses import dataclass
 
 import numpy as np
 
 from .engine import RasterInfo
 
 
-@dataclass
-class _Burn:
-    """What the dense replay needs: the inputs of the sparse call."""
-
-    table: object
-    values: object
-    fn: str
-    dtype: str
-    background: object
-    bands: np.ndarray | None
-    all_touched: bool
-
-
 class SparseArray:
     """A sparse array in COOrdinate format storing the band/row/col value
     triplets of all burned geometries."""
 
-    def __init__(self, band_names, band_counts, rows, cols, values, info: RasterInfo, burn: _Burn):
+    def __init__(self, band_names, band_counts, rows, cols, values, info: RasterInfo, fn: str, background):
         self._band_names = list(band_names)
         self._offsets = np.asarray(band_counts, dtype=np.uint64)
-        self.rows = rows
-        self.cols = cols
-        self.values = values
+        if len(self._offsets) != len(self._band_names):
+            raise ValueError("one triplet count per band is needed")
+        self.rows = np.ascontiguousarray(rows, dtype=np.uint64)
+        self.cols = np.ascontiguousarray(cols, dtype=np.uint64)
+        self.values = np.ascontiguousarray(values)
+        if not len(self.rows) == len(self.cols) == len(self.values) == int(self._offsets.sum()):
+            raise ValueError("rows, cols, values and the band counts disagree")
         self._info = info
-        self._burn = burn
+        self._fn = fn  # the pixel function and background the triplets replay with
+        self._background = background
 
     # ---- spatial information (arrays.rs:150-176) ----
     def band_names(self) -> list[str]:
@@ -66,7 +56,7 @@ class SparseArray:
     def size_hint(self) -> str:
         """Estimated size of the materialized dense array (pyarray.rs:77-91)."""
         nb, nr, nc = self.shape()
-        nbytes = np.dtype(self._burn.dtype).itemsize * nb * nr * nc
+        nbytes = self.values.dtype.itemsize * nb * nr * nc
         if nbytes < 1000:
             return f"{nbytes} bytes"
         f = np.float32(nbytes)  # the size is formatted from an f32 there
@@ -95,15 +85,14 @@ class SparseArray:
         out["values"] = self.values
         return out
 
-    def to_numpy(self) -> np.ndarray:
-        """build_array (arrays.rs:103-141): the writes replayed onto a
-        background raster with the pixel function."""
-        from .engine import rasterize_table
+    def to_numpy(self, *, context=None, stats: dict | None = None) -> np.ndarray:
+        """build_array (arrays.rs:103-141): the stored triplets replayed onto
+        a background raster with the pixel function, each pixel's writes in
+        stream order (on the GPU: ``rz_sparse_build``)."""
+        from .engine import sparse_build
 
-        b = self._burn
-        return rasterize_table(b.table, self._info, values=b.values, fn=b.fn, background=b.background,
-                               dtype=b.dtype, bands=b.bands, n_bands=len(self._band_names),
-                               all_touched=b.all_touched)
+        return sparse_build(self._offsets, self.rows, self.cols, self.values, self._info.nrows, self._info.ncols,
+                            fn=self._fn, background=self._background, context=context, stats=stats)
 
     def to_xarray(self):
         from ._native import _to_xarray

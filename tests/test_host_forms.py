@@ -10,7 +10,7 @@ import pytest
 from rusterize_gb300 import _lib
 from rusterize_gb300 import geometry as G
 from rusterize_gb300.engine import BatchJob, RasterInfo, _job_struct
-from rusterize_gb300.sparse import SparseArray, _Burn
+from rusterize_gb300.sparse import SparseArray
 
 
 def _info(nrows, ncols, epsg=None):
@@ -22,9 +22,8 @@ def _sparse(n_bands, nrows, ncols, dtype="float64", epsg=None):
     names = [f"b{i}" for i in range(n_bands)]
     counts = np.array([2] + [1] * (n_bands - 1), dtype=np.uint64)
     n = int(counts.sum())
-    burn = _Burn(table=None, values=None, fn="sum", dtype=dtype, background=0, bands=None, all_touched=False)
     return SparseArray(names, counts, np.arange(n, dtype=np.uint64), np.zeros(n, dtype=np.uint64),
-                       np.ones(n, dtype=dtype), _info(nrows, ncols, epsg), burn)
+                       np.ones(n, dtype=dtype), _info(nrows, ncols, epsg), "sum", 0)
 
 
 @pytest.mark.parametrize("shape,dtype,hint", [
