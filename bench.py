@@ -11,7 +11,9 @@ into uint32 (background 0).
           and rasters left on the device, CUDA events on the engine stream
   e2e   : the same metric through the public host API (rasterize_table) from
           pinned host buffers, H2D of the geometry and D2H of both rasters
-          inside the timed region
+          inside the timed region; the two burns are issued from two host
+          threads on their own contexts, like the reference arm's two
+          threads (the one-thread figure is reported beside it)
   cpu_baseline / --impl reference : the CPU restatement of the reference
           (oracle/), timed on this host on the same workload
 
@@ -334,26 +336,53 @@ def run_gb300(args) -> None:
         o_cnt = pinned(np.empty((1, nr, info.ncols), np.uint32), fill=False)
 
         e_stats: list = []
+        # The two burns of a step as two independent calls, each on its own
+        # engine context (stream), from two host threads -- the way the
+        # reference arm runs them -- so that one call's host->device upload
+        # and kernels overlap the other's device->host copy.  With
+        # --e2e-threads 1 they run one after the other on one context.
+        import concurrent.futures as cf
 
-        def host_step(keep=False):
-            s1, s2 = {}, {}
+        ctx2 = _lib.Context(local) if args.e2e_threads > 1 else ctx
+        pool = cf.ThreadPoolExecutor(2) if args.e2e_threads > 1 else None
+
+        def burn_sum(st):
             rz.rasterize_table(ptab, info, values=pvals, fn="sum", background=np.nan, dtype="float64", out=o_sum,
-                               context=ctx, stats=s1, rows=rows)
+                               context=ctx, stats=st, rows=rows)
+
+        def burn_count(st):
             rz.rasterize_table(ptab, info, values=None, fn="count", background=0, dtype="uint32", out=o_cnt,
-                               context=ctx, stats=s2, rows=rows)
+                               context=ctx2, stats=st, rows=rows)
+
+        def host_step(keep=False, threads=args.e2e_threads):
+            s1, s2 = {}, {}
+            if threads > 1:
+                f1, f2 = pool.submit(burn_sum, s1), pool.submit(burn_count, s2)
+                f1.result()
+                f2.result()
+            else:
+                burn_sum(s1)
+                burn_count(s2)
             if keep:
                 e_stats.append((s1, s2))
 
-        host_step()
-        barrier()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.e2e_steps):
-            host_step(keep=True)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        e_ms = max_over_ranks(e0.elapsed_time(e1) / args.e2e_steps, device=dev)
+        def timed_steps(threads):
+            host_step(threads=threads)
+            barrier()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e_stats.clear()
+            e0.record(stream)
+            for _ in range(args.e2e_steps):
+                host_step(keep=True, threads=threads)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return max_over_ranks(e0.elapsed_time(e1) / args.e2e_steps, device=dev)
+
+        e_ms_seq = timed_steps(1) if args.e2e_threads > 1 else None
+        e_ms = timed_steps(args.e2e_threads)
+        if pool is not None:
+            pool.shutdown()
         h2d = sum(a.nbytes for a in (tb.part_offsets, tb.part_kind, tb.ring_offsets, tb.vertex_offsets, tb.xy))
         h2d = 2 * h2d + values.nbytes
         d2h = o_sum.nbytes + o_cnt.nbytes
@@ -368,7 +397,9 @@ def run_gb300(args) -> None:
                "ms_h2d_per_step": ms_h2d, "ms_d2h_tail_per_step": ms_d2h, "ms_engine_per_step": ms_dev,
                "h2d_gbs": h2d / (ms_h2d / 1e3) / 1e9 if ms_h2d > 0 else None,
                "host_link_gbs": (h2d + d2h) / (e_ms / 1e3) / 1e9,
-               "buffers": "pinned host memory (torch pin_memory)"}
+               "buffers": "pinned host memory (torch pin_memory)",
+               "host_threads": args.e2e_threads,
+               "sequential_ms_per_step": e_ms_seq}
 
     peaks = _measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
@@ -628,6 +659,8 @@ def main():
                     help="N > 1: independent jobs per rank (weak scaling) or row bands of one job (strong)")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-threads", type=int, default=2, choices=[1, 2],
+                    help="host threads issuing the two burns of an e2e step (2: concurrent, own contexts)")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--batch-jobs", type=int, default=4096, help="jobs of the batched leg (0: skip it)")
