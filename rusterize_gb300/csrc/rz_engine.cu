@@ -779,6 +779,7 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
         FillArgs fa;
         fa.offsets = boff;
         fa.recs = sorted;
+        fa.brecs = reinterpret_cast<uint2*>(sb.wid);  // free once the records are scattered
         fa.pvals = d_values ? at(o_pval) : nullptr;
         fa.nbuckets = nbuckets;
         fa.scalar = scalar_bits;
@@ -1449,6 +1450,7 @@ static rz_status noalloc_impl(void* stream, const rz_geoms* g, const void* value
   FillArgs fa;
   fa.offsets = boff;
   fa.recs = sorted;
+  fa.brecs = reinterpret_cast<uint2*>(sb.wid);  // free once the records are scattered
   fa.pvals = d_vals_na ? at(o_pval) : nullptr;
   fa.nbuckets = nbuckets;
   fa.scalar = scalar_bits;
@@ -1795,6 +1797,7 @@ rz_status run_wave(rz_context* ctx, const rz_job* jobs, std::vector<BatchJob>& w
           FillArgs fa;
           fa.offsets = boff + lo;
           fa.recs = sorted;
+          fa.brecs = reinterpret_cast<uint2*>(sb.wid);  // free once the records are scattered
           fa.pvals = at(o_pval);
           fa.nbuckets = hi - lo;
           fa.scalar = 0;

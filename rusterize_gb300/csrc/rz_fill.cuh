@@ -26,6 +26,8 @@ struct FillJob {
 struct FillArgs {
   const unsigned* offsets;  // [nbuckets + 1]
   const uint2* recs;        // {part | word << REC_W_SHIFT | DEDUP_BIT, mask} grouped by bucket
+  uint2* brecs;             // scratch of the records' size: the deep buckets' records grouped by word, at
+                            // the records' own positions (nullptr: the per-word kernel scans whole buckets)
   const void* pvals;        // burn value of each part (T), or nullptr: every record burns `scalar`
   unsigned long long nbuckets;
   unsigned long long scalar;  // raw bits of the single value when pvals == nullptr
@@ -542,6 +544,82 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
   }
 }
 
+// ---- deep buckets: records grouped by word ------------------------------
+// One warp per deep bucket (the `big` list k_fill_warp leaves) counts the
+// bucket's records per word and copies them, grouped by word in word order,
+// to the same positions of `brecs`.  The per-(bucket, word) warps then find
+// their word's records by a binary search and read only those, instead of
+// scanning the whole bucket (sixteen words, twice each).  The order within
+// a word is not kept; the per-word kernel orders by part itself.
+constexpr int BIN_WARPS = 8;
+
+static __global__ void __launch_bounds__(BIN_WARPS * 32) k_big_bin(FillArgs a) {
+  __shared__ unsigned s_pos[BIN_WARPS][WPT];
+  const Ctrl* ctrl = a.ctrl;
+  if (ctrl->err || ctrl->span_count > a.rec_cap) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned* pos = s_pos[warp];
+  const unsigned nbig = *a.nbig;
+  const unsigned nwarps = gridDim.x * BIN_WARPS;
+  for (unsigned it = blockIdx.x * BIN_WARPS + warp; it < nbig; it += nwarps) {
+    const unsigned b = a.big[it];
+    const unsigned o0 = a.offsets[b];
+    const unsigned n = a.offsets[b + 1] - o0;
+    unsigned cnt = 0;  // lane w < WPT: records of word w
+    for (unsigned i0 = 0; i0 < n; i0 += 32) {
+      const unsigned i = i0 + lane;
+      const unsigned w = i < n ? (a.recs[o0 + i].x >> REC_W_SHIFT) & 15u : 0xFFu;
+#pragma unroll
+      for (int k = 0; k < WPT; ++k) {
+        const unsigned c = __popc(__ballot_sync(0xFFFFFFFFu, w == (unsigned)k));
+        if (lane == k) cnt += c;
+      }
+    }
+    unsigned incl = cnt;  // inclusive scan over lanes 0..WPT-1
+#pragma unroll
+    for (int o = 1; o < WPT; o <<= 1) {
+      const unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane < WPT) pos[lane] = incl - cnt;
+    __syncwarp();
+    for (unsigned i0 = 0; i0 < n; i0 += 32) {
+      const unsigned i = i0 + lane;
+      uint2 r = make_uint2(0u, 0u);
+      unsigned w = 0xFFu;
+      if (i < n) {
+        r = a.recs[o0 + i];
+        w = (r.x >> REC_W_SHIFT) & 15u;
+      }
+      const unsigned peers = __match_any_sync(0xFFFFFFFFu, w);
+      const int leader = __ffs(peers) - 1;
+      const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+      unsigned base = 0;
+      if (lane == leader && w < (unsigned)WPT) base = atomicAdd(&pos[w], (unsigned)__popc(peers));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (w < (unsigned)WPT) a.brecs[o0 + base + rank] = r;
+    }
+    __syncwarp();
+  }
+}
+
+// The records of word `wsel` in a deep bucket grouped by k_big_bin: the
+// range [lo, hi) of [0, n) whose word is wsel (binary searches on the word).
+__device__ __forceinline__ void word_range(const uint2* r, unsigned n, unsigned wsel, unsigned& lo, unsigned& hi) {
+  unsigned l = 0, h = n;  // first index whose word is >= wsel
+  while (l < h) {
+    const unsigned m = (l + h) >> 1;
+    if (((r[m].x >> REC_W_SHIFT) & 15u) < wsel) l = m + 1; else h = m;
+  }
+  lo = l;
+  h = n;  // first index whose word is > wsel
+  while (l < h) {
+    const unsigned m = (l + h) >> 1;
+    if (((r[m].x >> REC_W_SHIFT) & 15u) <= wsel) l = m + 1; else h = m;
+  }
+  hi = l;
+}
+
 // ---- deep buckets: one warp per (bucket, word) --------------------------
 // The word's records are taken in part order, at most BIG_CAP at a time: a
 // histogram over the pending part ids picks the largest prefix range that
@@ -636,8 +714,16 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
   for (unsigned long long it = (unsigned long long)blockIdx.x * BIG_WARPS + warp; it < items; it += nwarps) {
     const unsigned long long b = a.big[it / WPT];
     const unsigned wsel = (unsigned)(it % WPT);
-    const unsigned o0 = a.offsets[b];
-    const int n = (int)(a.offsets[b + 1] - o0);
+    unsigned o0 = a.offsets[b];
+    int n = (int)(a.offsets[b + 1] - o0);
+    const uint2* recs = a.recs;
+    if (a.brecs) {  // only this word's records, from the grouped copy
+      unsigned lo, hi;
+      word_range(a.brecs + o0, (unsigned)n, wsel, lo, hi);
+      recs = a.brecs;
+      o0 += lo;
+      n = (int)(hi - lo);
+    }
     int len;
     T* dst = bucket_tile<T>(a, b, len);
     const int x = (int)wsel * 32 + lane;
@@ -647,7 +733,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
     while (true) {
       unsigned cnt = 0, pmin = 0xFFFFFFFFu, pmax = 0;
       for (int i = lane; i < n; i += 32) {
-        const unsigned rx = a.recs[o0 + i].x;
+        const unsigned rx = recs[o0 + i].x;
         const unsigned part = rx & REC_PART_MASK;
         if (((rx >> REC_W_SHIFT) & 15u) == wsel && part >= lo_part) {
           ++cnt;
@@ -669,7 +755,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
           for (int h = lane; h < BIG_HIST; h += 32) hist[h] = 0u;
           __syncwarp();
           for (int i = lane; i < n; i += 32) {
-            const unsigned rx = a.recs[o0 + i].x;
+            const unsigned rx = recs[o0 + i].x;
             const unsigned part = rx & REC_PART_MASK;
             if (((rx >> REC_W_SHIFT) & 15u) == wsel && part >= span_lo && part <= span_hi)
               atomicAdd(&hist[(part - span_lo) >> shift], 1u);
@@ -706,7 +792,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
         uint2 r = make_uint2(0u, 0u);
         bool take = false;
         if (i < n) {
-          r = a.recs[o0 + i];
+          r = recs[o0 + i];
           const unsigned part = r.x & REC_PART_MASK;
           take = ((r.x >> REC_W_SHIFT) & 15u) == wsel && part >= lo_part && part < hi;
         }
@@ -858,6 +944,10 @@ int launch_fill_t(const FillArgs& a, int fn, bool dedup, int num_sms, cudaStream
     const unsigned grid =                                                                                 \
         persistent((const void*)k_fill_warp<T, FNV, DD>, FILL_WARPS_PER_BLOCK * 32, ws, FILL_WARPS_PER_BLOCK); \
     k_fill_warp<T, FNV, DD><<<grid, FILL_WARPS_PER_BLOCK * 32, ws, s>>>(a);                               \
+    if (a.brecs) {                                                                                        \
+      k_big_bin<<<num_sms * 2, BIN_WARPS * 32, 0, s>>>(a);                                                \
+      ++launches;                                                                                         \
+    }                                                                                                     \
     k_fill_big<T, FNV, DD><<<num_sms * 4, BIG_WARPS * 32, bs, s>>>(a);                                    \
     launches += 2;                                                                                        \
   }
