@@ -191,6 +191,60 @@ __device__ __forceinline__ T rec_value(const FillArgs& a, unsigned rec_x) {
   return from_bits<T>(a.scalar);
 }
 
+// ---- order-free first / last ---------------------------------------------
+// `last` leaves a pixel at the value of the largest part that writes it.
+// `first` takes the first write and keeps it unless it is the background or
+// NaN (pixel_functions.rs:56-122), and every part writes one value: so the
+// pixel ends at the value of the smallest part whose value is neither
+// ("sticky"), or -- when no written value is sticky -- at the value of the
+// largest part (every write replaced the one before).  Both are reductions
+// over the parts that write the pixel, and need no sort: one pass over the
+// records in any order keeps, per pixel, the largest part (+1, 0 = none) and,
+// for `first`, the smallest sticky part (~0u = none).
+constexpr int OF_WARP_MAX = 1024;  // deeper buckets go to the per-word kernel
+
+template <typename T>
+__device__ __forceinline__ T part_value(const FillArgs& a, unsigned p) {
+  if (a.pvals) return static_cast<const T*>(a.pvals)[p];
+  return from_bits<T>(a.scalar);
+}
+
+template <typename T>
+__device__ __forceinline__ bool first_resets(T v, T bg, const BgF64& bgc) {
+  if constexpr (std::is_same<T, double>::value) {
+    const unsigned long long b = f64_bits(v);
+    return eq_bg_f64(b, bgc) || nan_bits(b);
+  } else {
+    return v == bg || is_nan_v(v);
+  }
+}
+
+// A record for the order-free pass: the part, bit 31 set when its value is
+// sticky for `first` (the DEDUP flag plays no role for first / last: a part
+// writes one value, so repeated writes of a part change nothing).
+template <typename T, int FN>
+__device__ __forceinline__ unsigned of_key(const FillArgs& a, unsigned rx, T bg, const BgF64& bgc) {
+  unsigned k = rx & REC_PART_MASK;
+  if constexpr (FN == F_FIRST) {
+    if (!first_resets<T>(rec_value<T>(a, rx), bg, bgc)) k |= DEDUP_BIT;
+  }
+  return k;
+}
+
+template <int FN>
+__device__ __forceinline__ void of_update(unsigned& maxp1, unsigned& ming, unsigned k) {
+  const unsigned p = k & REC_PART_MASK;
+  maxp1 = max(maxp1, p + 1u);
+  if (FN == F_FIRST && (k & DEDUP_BIT)) ming = min(ming, p);
+}
+
+template <typename T, int FN>
+__device__ __forceinline__ T of_result(const FillArgs& a, unsigned maxp1, unsigned ming, T bg) {
+  if (FN == F_FIRST && ming != 0xFFFFFFFFu) return part_value<T>(a, ming);
+  if (maxp1 == 0u) return bg;
+  return part_value<T>(a, maxp1 - 1u);
+}
+
 template <typename T>
 __device__ __forceinline__ T shfl_val(T v, int src) {
   if constexpr (sizeof(T) == 8) {
@@ -473,6 +527,49 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
         store_bg<T>(dst, len, a.bg16, bg, lane, 32);
         continue;
       }
+      if constexpr (FN == F_FIRST || FN == F_LAST) {
+        if (n > OF_WARP_MAX) {
+          if (lane == 0) a.big[atomicAdd(a.nbig, 1u)] = (unsigned)b;
+          continue;
+        }
+        // per pixel (word w, lane l) at w * 32 + l: each lane owns its
+        // column, so the pass needs no synchronisation
+        unsigned* smax = reinterpret_cast<unsigned*>(srec);
+        unsigned* smin = smax + WPT * 32;
+#pragma unroll
+        for (int w = 0; w < WPT; ++w) {
+          smax[w * 32 + lane] = 0u;
+          if (FN == F_FIRST) smin[w * 32 + lane] = 0xFFFFFFFFu;
+        }
+        for (int i0 = 0; i0 < n; i0 += 32) {
+          const int i = i0 + lane;
+          unsigned kx = 0u, km = 0u, kw = 0u;
+          if (i < n) {
+            const uint2 r = a.recs[o_cur + i];
+            kx = of_key<T, FN>(a, r.x, bg, bgc);
+            km = r.y;
+            kw = (r.x >> REC_W_SHIFT) & 15u;
+          }
+          const int cnt = min(32, n - i0);
+          for (int j = 0; j < cnt; ++j) {
+            const unsigned xj = __shfl_sync(0xFFFFFFFFu, kx, j), mj = __shfl_sync(0xFFFFFFFFu, km, j);
+            const unsigned wj = __shfl_sync(0xFFFFFFFFu, kw, j);
+            if ((mj >> lane) & 1u) {
+              const unsigned ix = wj * 32u + (unsigned)lane;
+              unsigned mx = smax[ix], mn = FN == F_FIRST ? smin[ix] : 0u;
+              of_update<FN>(mx, mn, xj);
+              smax[ix] = mx;
+              if (FN == F_FIRST) smin[ix] = mn;
+            }
+          }
+        }
+#pragma unroll
+        for (int w = 0; w < WPT; ++w) {
+          const int x = w * 32 + lane;
+          if (x < len) dst[x] = of_result<T, FN>(a, smax[x], FN == F_FIRST ? smin[x] : 0xFFFFFFFFu, bg);
+        }
+        continue;
+      }
       if (n > FILL_WARP_MAX) {
         if (n > a.sort_max) {
           if (lane == 0) a.big[atomicAdd(a.nbig, 1u)] = (unsigned)b;
@@ -727,6 +824,25 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
     int len;
     T* dst = bucket_tile<T>(a, b, len);
     const int x = (int)wsel * 32 + lane;
+    if constexpr (FN == F_FIRST || FN == F_LAST) {  // order-free: one pass, no sort
+      unsigned maxp1 = 0u, ming = 0xFFFFFFFFu;
+      for (int i0 = 0; i0 < n; i0 += 32) {
+        const int i = i0 + lane;
+        unsigned kx = 0u, km = 0u;
+        if (i < n) {
+          const uint2 r = recs[o0 + i];
+          kx = of_key<T, FN>(a, r.x, bg, bgc);
+          km = ((r.x >> REC_W_SHIFT) & 15u) == wsel ? r.y : 0u;
+        }
+        const int cnt = min(32, n - i0);
+        for (int j = 0; j < cnt; ++j) {
+          const unsigned xj = __shfl_sync(0xFFFFFFFFu, kx, j), mj = __shfl_sync(0xFFFFFFFFu, km, j);
+          if ((mj >> lane) & 1u) of_update<FN>(maxp1, ming, xj);
+        }
+      }
+      if (x < len) dst[x] = of_result<T, FN>(a, maxp1, ming, bg);
+      continue;
+    }
     T c = bg;
     unsigned last_part = 0xFFFFFFFFu;
     unsigned lo_part = 0;  // parts < lo_part are done
