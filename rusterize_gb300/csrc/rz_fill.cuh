@@ -245,6 +245,27 @@ __device__ __forceinline__ T of_result(const FillArgs& a, unsigned maxp1, unsign
   return part_value<T>(a, maxp1 - 1u);
 }
 
+// `min` / `max` (cur == bg || NaN || cur > v, resp. < v) are order-free
+// too when no written value is the background or NaN: after the first write
+// every step keeps the running minimum (maximum) and an equal value does not
+// replace it, so the pixel ends at the value of the smallest part among those
+// whose value equals the extreme (only -0.0 and +0.0 are equal with other
+// bits).  A pass that meets such a value falls back to the sorted fold.
+template <typename T, int FN>
+__device__ __forceinline__ bool of_better(T v, unsigned p, T bv, unsigned bp) {
+  if (bp == 0xFFFFFFFFu) return true;
+  bool ahead, eq;
+  if constexpr (std::is_same<T, double>::value) {
+    const unsigned long long x = f64_bits(v), y = f64_bits(bv);
+    ahead = FN == F_MIN ? gt_f64(y, x) : gt_f64(x, y);
+    eq = x == y || ((x | y) & 0x7FFFFFFFFFFFFFFFull) == 0;
+  } else {
+    ahead = FN == F_MIN ? v < bv : v > bv;
+    eq = v == bv;
+  }
+  return ahead || (eq && p < bp);
+}
+
 template <typename T>
 __device__ __forceinline__ T shfl_val(T v, int src) {
   if constexpr (sizeof(T) == 8) {
@@ -570,6 +591,51 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
         }
         continue;
       }
+      if constexpr (FN == F_MIN || FN == F_MAX) {
+        if (n <= OF_WARP_MAX) {
+          // per pixel (word w, lane l) at w * 32 + l: its extreme and part
+          T* sval = reinterpret_cast<T*>(srec);
+          unsigned* spart = reinterpret_cast<unsigned*>(sval + WPT * 32);
+#pragma unroll
+          for (int w = 0; w < WPT; ++w) spart[w * 32 + lane] = 0xFFFFFFFFu;
+          bool bad = false;
+          for (int i0 = 0; i0 < n; i0 += 32) {
+            const int i = i0 + lane;
+            unsigned kx = 0u, km = 0u;
+            T kv = T(0);
+            if (i < n) {
+              const uint2 r = a.recs[o_cur + i];
+              kv = rec_value<T>(a, r.x);
+              kx = r.x;
+              km = r.y;
+              bad = bad || first_resets<T>(kv, bg, bgc);
+            }
+            if (__any_sync(0xFFFFFFFFu, bad)) break;
+            const int cnt = min(32, n - i0);
+            for (int j = 0; j < cnt; ++j) {
+              const unsigned xj = __shfl_sync(0xFFFFFFFFu, kx, j), mj = __shfl_sync(0xFFFFFFFFu, km, j);
+              const T vj = shfl_val<T>(kv, j);
+              if ((mj >> lane) & 1u) {
+                const unsigned ix = ((xj >> REC_W_SHIFT) & 15u) * 32u + (unsigned)lane;
+                const unsigned pj = xj & REC_PART_MASK;
+                if (of_better<T, FN>(vj, pj, sval[ix], spart[ix])) {
+                  sval[ix] = vj;
+                  spart[ix] = pj;
+                }
+              }
+            }
+          }
+          if (!__any_sync(0xFFFFFFFFu, bad)) {
+#pragma unroll
+            for (int w = 0; w < WPT; ++w) {
+              const int x = w * 32 + lane;
+              if (x < len) dst[x] = spart[x] == 0xFFFFFFFFu ? bg : sval[x];
+            }
+            continue;
+          }
+          __syncwarp();  // the sorted fold below reuses the shared memory
+        }
+      }
       if (n > FILL_WARP_MAX) {
         if (n > a.sort_max) {
           if (lane == 0) a.big[atomicAdd(a.nbig, 1u)] = (unsigned)b;
@@ -842,6 +908,42 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
       }
       if (x < len) dst[x] = of_result<T, FN>(a, maxp1, ming, bg);
       continue;
+    }
+    if constexpr (FN == F_MIN || FN == F_MAX) {  // order-free unless a value resets the pixel
+      T bv = bg;
+      unsigned bp = 0xFFFFFFFFu;
+      bool bad = false;
+      for (int i0 = 0; i0 < n; i0 += 32) {
+        const int i = i0 + lane;
+        unsigned kx = 0u, km = 0u;
+        T kv = T(0);
+        if (i < n) {
+          const uint2 r = recs[o0 + i];
+          if (((r.x >> REC_W_SHIFT) & 15u) == wsel) {
+            kv = rec_value<T>(a, r.x);
+            kx = r.x;
+            km = r.y;
+            bad = bad || first_resets<T>(kv, bg, bgc);
+          }
+        }
+        if (__any_sync(0xFFFFFFFFu, bad)) break;
+        const int cnt = min(32, n - i0);
+        for (int j = 0; j < cnt; ++j) {
+          const unsigned xj = __shfl_sync(0xFFFFFFFFu, kx, j), mj = __shfl_sync(0xFFFFFFFFu, km, j);
+          const T vj = shfl_val<T>(kv, j);
+          if ((mj >> lane) & 1u) {
+            const unsigned pj = xj & REC_PART_MASK;
+            if (of_better<T, FN>(vj, pj, bv, bp)) {
+              bv = vj;
+              bp = pj;
+            }
+          }
+        }
+      }
+      if (!__any_sync(0xFFFFFFFFu, bad)) {
+        if (x < len) dst[x] = bv;
+        continue;
+      }
     }
     T c = bg;
     unsigned last_part = 0xFFFFFFFFu;

@@ -186,6 +186,34 @@ def test_big_buckets_ordered():
     check(t, grid, fn="count", values=None, background=0, dtype="uint16")
 
 
+@pytest.mark.parametrize("fn", ["first", "last", "min", "max"])
+@pytest.mark.parametrize("dtype", ["int16", "float32", "float64"])
+def test_order_free_folds_ties_and_resets(fn, dtype):
+    """first / last / min / max fold without a sort unless a written value is
+    the background or NaN: equal values (-0.0 and +0.0 among them) go to the
+    earliest part, and a value equal to the background, or NaN, sends the tile
+    back to the sorted fold.  300 polygons over 64 x 64 give tiles of a few
+    hundred records (one warp per tile), 6,000 give tiles of thousands (one
+    warp per word)."""
+    rng = np.random.default_rng(zlib.crc32(f"of/{fn}/{dtype}".encode()))
+    grid = dict(nrows=64, ncols=64, xmin=0.0, xmax=64.0, ymin=0.0, ymax=64.0, xres=1.0, yres=1.0)
+    floating = np.dtype(dtype).kind == "f"
+    for n in (300, 6000):
+        t = synth.star_polygons(rng, n, (3, 12), rng.uniform(3, 30, n), rng.uniform(0, 64, n), rng.uniform(0, 64, n))
+        for bg in ((np.nan, 0.0) if floating else (0, 3)):
+            if floating:
+                clean = [x for x in (0.0, -0.0, 1.0, -1.0, 2.5) if not x == bg]
+                dirty = clean + [bg, np.nan]
+            else:
+                clean = [x for x in (0, 1, 2, 5, -1) if x != bg]
+                dirty = clean + [bg]
+            for pool in (clean, dirty):
+                v = rng.choice(np.array(pool, dtype=dtype), n)
+                stats = check(t, grid, fn=fn, values=v, background=bg, dtype=dtype)
+                if n == 6000:
+                    assert stats["big_buckets"] > 0
+
+
 def test_single_part_many_spans_in_one_bucket():
     # one zig-zag polygon with > 4096 spans in a single row tile
     k = 5000
