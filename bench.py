@@ -119,6 +119,23 @@ class Clocks:
                 "samples": len(sm)}
 
 
+class _nvtx:
+    """An NVTX range around a leg, so that a profiler can select its launches."""
+
+    def __init__(self, name: str):
+        self.name = name
+
+    def __enter__(self):
+        import torch
+
+        torch.cuda.nvtx.range_push(self.name)
+
+    def __exit__(self, *a):
+        import torch
+
+        torch.cuda.nvtx.range_pop()
+
+
 def _measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -298,7 +315,7 @@ def run_gb300(args) -> None:
     barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(local) as clk:
+    with Clocks(local) as clk, _nvtx("large_fill"):
         ev0.record(stream)
         for _ in range(args.steps):
             step(acc)
@@ -522,12 +539,14 @@ def _batched_leg(args, ctx, local) -> dict:
     if "plain" in legs:
         if args.tune:
             tunings["plain"] = tune.autotune(ctx, plain_sample_ms, rounds=1, repeats=1, warmup=1).as_dict()
-        ms_plain = timed(plain, args.batch_steps)
+        with _nvtx("batch_plain"):
+            ms_plain = timed(plain, args.batch_steps)
     if "batched" in legs:
         if args.tune:
             ctx.set_tuning(None)
             tunings["batched"] = tune.autotune(ctx, batch_sample_ms, rounds=2, repeats=2, warmup=1).as_dict()
-        ms_batch = timed(batch, args.batch_steps)
+        with _nvtx("batch_batched"):  # ncu --nvtx --nvtx-include "batch_batched/" selects these launches
+            ms_batch = timed(batch, args.batch_steps)
     ctx.set_tuning(None)
     n = len(jobs)
     out = {
