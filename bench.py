@@ -516,6 +516,9 @@ def _batched_leg(args, ctx, local) -> dict:
     # each leg runs with its own schedule, tuned on a sample of the jobs
     from rusterize_gb300 import tune
 
+    # the plain leg is tuned on a sample (one call per job is slow); the
+    # batched leg, one call over all jobs in well under a second, on the
+    # whole batch
     ns = min(len(jobs), max(1, args.batch_tune_jobs))
     sample_j, sample_o = jobs[:ns], outs[:ns]
 
@@ -528,9 +531,9 @@ def _batched_leg(args, ctx, local) -> dict:
             tot += st1["ms_device_total"]
         return tot
 
-    def batch_sample_ms():
+    def batch_ms():
         st1: dict = {}
-        rasterize_batch_device(sample_j, dtype="float32", outs=sample_o, context=ctx, stats=st1)
+        rasterize_batch_device(jobs, dtype="float32", outs=outs, context=ctx, stats=st1)
         return st1["ms_device_total"]
 
     legs = set(args.batch_legs.split(","))
@@ -544,7 +547,7 @@ def _batched_leg(args, ctx, local) -> dict:
     if "batched" in legs:
         if args.tune:
             ctx.set_tuning(None)
-            tunings["batched"] = tune.autotune(ctx, batch_sample_ms, rounds=2, repeats=2, warmup=1).as_dict()
+            tunings["batched"] = tune.autotune(ctx, batch_ms, rounds=2, repeats=2, warmup=1).as_dict()
         with _nvtx("batch_batched"):  # ncu --nvtx --nvtx-include "batch_batched/" selects these launches
             ms_batch = timed(batch, args.batch_steps)
     ctx.set_tuning(None)
@@ -556,7 +559,7 @@ def _batched_leg(args, ctx, local) -> dict:
         "batched": {"ms": ms_batch, "jobs_per_s": n / (ms_batch / 1e3), "px_per_s": px / (ms_batch / 1e3),
                     "waves": st.get("waves"), "kernel_launches": st.get("kernel_launches")},
         "batched_over_plain": ms_plain / ms_batch,
-        "tuning": dict(tunings, sample_jobs=ns,
+        "tuning": dict(tunings, sample_jobs={"plain": ns, "batched": n},
                        workload_class=tune.batch_class(n, px, sum(j.table.table.n_geoms for j in jobs),
                                                        sum(j.table.table.n_vertices for j in jobs))),
         "note": "device-resident geometry and rasters; CUDA events on the engine stream; outputs larger than L2",
@@ -691,7 +694,8 @@ def main():
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--batch-jobs", type=int, default=4096, help="jobs of the batched leg (0: skip it)")
-    ap.add_argument("--batch-tune-jobs", type=int, default=256, help="jobs of the sample each batched leg is tuned on")
+    ap.add_argument("--batch-tune-jobs", type=int, default=512,
+                    help="jobs of the sample the plain leg is tuned on (the batched leg is tuned on all jobs)")
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="run with the default schedule")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--batch-warmup", type=int, default=1)
