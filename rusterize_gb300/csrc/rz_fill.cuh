@@ -1051,13 +1051,27 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
 // warp and lane l adds its bit l to the counter of the record's word.
 constexpr int DEPTH_WARPS = 8;
 
+// 32 x 32 bit transpose across a warp: lane i holds row i on entry and
+// column l (bit i = bit l of row i) in lane l on return.  Five butterfly
+// stages, each swapping the off-diagonal j x j blocks of every 2j x 2j block.
+__device__ __forceinline__ unsigned warp_transpose32(unsigned x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int j = 16 >> s;
+    const unsigned m = s == 0 ? 0x0000FFFFu : s == 1 ? 0x00FF00FFu : s == 2 ? 0x0F0F0F0Fu : s == 3 ? 0x33333333u
+                                                                                                    : 0x55555555u;
+    const unsigned y = __shfl_xor_sync(0xFFFFFFFFu, x, j);
+    x = (lane & j) ? ((x & ~m) | ((y >> j) & m)) : ((x & m) | ((y << j) & ~m));
+  }
+  return x;
+}
+
 template <typename T, int FN>
 __global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
-  __shared__ unsigned s_cnt[DEPTH_WARPS][WPT * 32];
   Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned* cnt = s_cnt[warp];
+  const int lane = threadIdx.x & 31;
   const T bg = from_bits<T>(a.bg);
   const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
   while (true) {
@@ -1088,24 +1102,23 @@ __global__ void __launch_bounds__(DEPTH_WARPS * 32) k_fill_depth(FillArgs a) {
         store_bg<T>(dst, len, a.bg16, bg, lane, 32);
         continue;
       }
-      // lane l owns column l of the tile's 16 words: cnt[w * 32 + l], so the
-      // counters need no atomics and sit in distinct banks
+      // 32 records at a time, bit-sliced: after the transpose lane l holds
+      // bit l of every record's mask, so the depth of pixel (w, l) grows by
+      // the records of word w among those bits (lanes past the end hold an
+      // empty mask and add nothing)
+      unsigned c[WPT];
 #pragma unroll
-      for (int w = 0; w < WPT; ++w) cnt[w * 32 + lane] = 0u;
-      __syncwarp();
+      for (int w = 0; w < WPT; ++w) c[w] = 0u;
       for (int i0 = 0; i0 < n; i0 += 32) {
         if (i0 > 0) r = i0 + lane < n ? a.recs[o0 + i0 + lane] : make_uint2(0u, 0u);
-        const int m = min(32, n - i0);
-        for (int i = 0; i < m; ++i) {
-          const unsigned x = __shfl_sync(0xFFFFFFFFu, r.x, i);
-          const unsigned y = __shfl_sync(0xFFFFFFFFu, r.y, i);
-          if ((y >> lane) & 1u) ++cnt[((x >> REC_W_SHIFT) & 15u) * 32 + lane];
-        }
+        const unsigned wd = (r.x >> REC_W_SHIFT) & 15u;
+        const unsigned t = warp_transpose32(r.y);
+#pragma unroll
+        for (int w = 0; w < WPT; ++w) c[w] += (unsigned)__popc(t & __ballot_sync(0xFFFFFFFFu, wd == (unsigned)w));
       }
-      __syncwarp();
 #pragma unroll
       for (int w = 0; w < WPT; ++w) {
-        const unsigned d = cnt[w * 32 + lane];
+        const unsigned d = c[w];
         T v = bg;
         if (d) {
           if constexpr (FN == F_ANY) v = T(1);
