@@ -301,7 +301,10 @@ def run_gb300(args) -> None:
     # the engine's schedule for this workload class, chosen by the autotuner
     # (outside the timed region; results do not depend on it)
     tuning = None
-    if args.tune:
+    if args.schedule:
+        ctx.set_tuning(json.loads(args.schedule))
+        tuning = {"tuning": ctx.tuning, "fixed": True}
+    elif args.tune:
         from rusterize_gb300 import tune
 
         def step_ms():
@@ -697,6 +700,8 @@ def main():
     ap.add_argument("--batch-tune-jobs", type=int, default=512,
                     help="jobs of the sample the plain leg is tuned on (the batched leg is tuned on all jobs)")
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="run with the default schedule")
+    ap.add_argument("--schedule", default=None,
+                    help='fixed schedule of the large-fill leg instead of tuning, e.g. \'{"fill_sort_max": 128}\'')
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--batch-warmup", type=int, default=1)
     ap.add_argument("--batch-legs", default="plain,batched", help="legs of the batched comparison to run")

@@ -181,7 +181,8 @@ typedef struct {
   uint32_t wide_blocks_per_sm;    /* wide span kernel blocks per SM (1..occupancy limit; the limit) */
   uint32_t rows_per_window;       /* polygon window height cap (8..128; 128) */
   uint32_t narrow_max_words;      /* widest window of the narrow kernel, in 32-pixel words (1..32; 32) */
-  uint32_t fill_sort_max;         /* records of one tile the warp fill sorts before the per-word path (64..256; 256) */
+  uint32_t fill_sort_max;         /* records of one tile the warp fill sorts before the per-word path (64..256; 256);
+                                     also sizes the warp fill's shared memory, so a smaller value fits more warps */
   uint32_t scatter_blocks_per_sm; /* record scatter blocks per SM (1..32; 8) */
   uint32_t line_blocks_per_sm;    /* line and point span kernels, blocks per SM (1..32; 8) */
 } rz_tuning;

@@ -40,6 +40,8 @@ struct FillArgs {
   Ctrl* ctrl;
   unsigned long long rec_cap;
   int sort_max;              // tiles of up to this many records are sorted by one warp (<= FILL_WARP_SORT)
+  int sort_cap;              // k_fill_warp: sort entries per warp (a power of two >= sort_max)
+  int warp_bytes;            // k_fill_warp: shared memory per warp
   unsigned long long* work;  // chunk counter of this fill (zero before the launch)
   unsigned* nbig;            // entries of `big` (zero before the launch)
   // bucket b of this fill is bucket bucket0 + b of the call (a fill may run
@@ -356,25 +358,45 @@ __device__ __forceinline__ void apply_step(T& c, T v, bool on, T bg, const BgF64
 }
 
 // ---- warp fill -------------------------------------------------------------
-// Buckets of at most FILL_WARP_MAX records, one warp each.  A warp takes 32
-// consecutive buckets (one coalesced load of their offsets) and loads the
-// next bucket's records and values while it works on the current one.
+// One warp per bucket.  A warp takes 32 consecutive buckets (one coalesced
+// load of their offsets) and loads the next bucket's records and values
+// while it works on the current one.
 //
 // Records of different words touch different pixels, so only the part
-// order within a word matters.  The records are sorted by (word, part) with
-// a bitonic network in registers (two records per lane) and then walked
-// once: lane l keeps pixel l of the current word in a register, applies
-// each record whose mask covers it, and stores the word when the walk moves
-// on (words without records are background).  A pixel-function step that
-// needs a float64 add issues it only when some lane of the warp needs it.
-// Records of one deduplicating part and word are adjacent in the order and
-// write a pixel once (PixelCache).
+// order within a word matters.  Up to FILL_WARP_MAX records are sorted by
+// (word, part) with a bitonic network in registers (two records per lane),
+// up to the schedule's sort_max in shared memory, and then walked once:
+// lane l keeps pixel l of the current word in a register, applies each
+// record whose mask covers it, and stores the word when the walk moves on
+// (words without records are background).  A pixel-function step that needs
+// a float64 add issues it only when some lane of the warp needs it.  Records
+// of one deduplicating part and word are adjacent in the order and write a
+// pixel once (PixelCache).  Deeper buckets go to the per-word kernel.
+//
+// first / last (buckets of up to OF_WARP_MAX records), and min / max when no
+// written value is the background or NaN, take the order-free pass instead.
 constexpr int FILL_WARPS_PER_BLOCK = 8;
 constexpr int FILL_CHUNK = 32;
 
+// Shared memory of one k_fill_warp warp: the sort's records and keys (a
+// power of two of entries, at least sort_max, so that the bitonic network's
+// padding stays inside), or the order-free pass's per-pixel state, whichever
+// is larger.  A smaller sort_max lets more warps share an SM.
+inline int fill_sort_cap(int sort_max) {
+  int e = FILL_WARP_MAX;
+  while (e < sort_max) e <<= 1;
+  return e;
+}
+
 template <typename T>
-constexpr int fill_warp_bytes() {
-  return FILL_WARP_SORT * ((int)sizeof(SRec) + 8);
+inline int fill_warp_bytes(int fn, int sort_cap) {
+  int b = sort_cap * ((int)sizeof(SRec) + 8);
+  if (fn == F_FIRST || fn == F_LAST) b = b > 2 * WPT * 32 * 4 ? b : 2 * WPT * 32 * 4;
+  if (fn == F_MIN || fn == F_MAX) {
+    const int m = WPT * 32 * ((int)sizeof(T) + 4);
+    b = b > m ? b : m;
+  }
+  return (b + 15) & ~15;
 }
 
 // the two records (positions lane and lane + 32) of a bucket held by a lane
@@ -516,7 +538,7 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
   Ctrl* ctrl = a.ctrl;
   if (ctrl->err || ctrl->span_count > a.rec_cap) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  SRec* srec = reinterpret_cast<SRec*>(smem + warp * fill_warp_bytes<T>());
+  SRec* srec = reinterpret_cast<SRec*>(smem + warp * a.warp_bytes);
   const T bg = from_bits<T>(a.bg);
   const BgF64 bgc = bg_f64(a.bg);
   const unsigned long long nchunks = (a.nbuckets + FILL_CHUNK - 1) / FILL_CHUNK;
@@ -641,10 +663,10 @@ __global__ void __launch_bounds__(FILL_WARPS_PER_BLOCK * 32) k_fill_warp(FillArg
           if (lane == 0) a.big[atomicAdd(a.nbig, 1u)] = (unsigned)b;
           continue;
         }
-        // up to FILL_WARP_SORT records: staged and sorted in shared memory,
+        // up to sort_max records: staged and sorted in shared memory,
         // key = (word, part) << 8 | position
         const unsigned o0 = o_cur;
-        unsigned long long* skey = reinterpret_cast<unsigned long long*>(srec + FILL_WARP_SORT);
+        unsigned long long* skey = reinterpret_cast<unsigned long long*>(srec + a.sort_cap);
         for (int i = lane; i < n; i += 32) {
           const uint2 r = a.recs[o0 + i];
           SRec e;
@@ -791,7 +813,8 @@ __device__ __forceinline__ void word_range(const uint2* r, unsigned n, unsigned 
 // records to the next one covering its pixel, so every step applies one
 // record per lane.  A single part with more than BIG_CAP records in the word
 // is applied in chunks (its records share one value and their order does
-// not change the result).
+// not change the result).  first / last, and min / max without a background
+// or NaN value among the word's records, take one order-free pass instead.
 constexpr int BIG_WARPS = 4;
 constexpr int BIG_HIST = 256;
 
@@ -1168,13 +1191,16 @@ int launch_fill_t(const FillArgs& a, int fn, bool dedup, int num_sms, cudaStream
   int launches = 0;
 #define RZ_FILL_CASE(FNV, DD)                                                                             \
   {                                                                                                       \
-    constexpr int ws = FILL_WARPS_PER_BLOCK * fill_warp_bytes<T>();                                       \
+    FillArgs aw = a;                                                                                      \
+    aw.sort_cap = fill_sort_cap(a.sort_max);                                                              \
+    aw.warp_bytes = fill_warp_bytes<T>(FNV, aw.sort_cap);                                                 \
+    const int ws = FILL_WARPS_PER_BLOCK * aw.warp_bytes;                                                  \
     constexpr int bs = BIG_WARPS * big_warp_bytes<T>();                                                   \
     cudaFuncSetAttribute(k_fill_warp<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws);       \
     cudaFuncSetAttribute(k_fill_big<T, FNV, DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, bs);        \
     const unsigned grid =                                                                                 \
         persistent((const void*)k_fill_warp<T, FNV, DD>, FILL_WARPS_PER_BLOCK * 32, ws, FILL_WARPS_PER_BLOCK); \
-    k_fill_warp<T, FNV, DD><<<grid, FILL_WARPS_PER_BLOCK * 32, ws, s>>>(a);                               \
+    k_fill_warp<T, FNV, DD><<<grid, FILL_WARPS_PER_BLOCK * 32, ws, s>>>(aw);                              \
     if (a.brecs) {                                                                                        \
       k_big_bin<<<num_sms * 2, BIN_WARPS * 32, 0, s>>>(a);                                                \
       ++launches;                                                                                         \
