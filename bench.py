@@ -42,6 +42,7 @@ sys.path.insert(0, str(ROOT))
 
 WORKLOAD = "large_fill_100k_polygons_20000x20000_sum_f64+count_u32"
 REF_THREADS = 2  # host threads of both CPU legs: one per burn of a step
+REF_BUDGET_S = 100.0  # CPU seconds of timed steps in the reference arm (full-size steps, at least three)
 METRIC = "burned px/s (large polygon fill: sum f64 + count u32)"
 
 
@@ -184,17 +185,22 @@ def run_reference(args) -> None:
 
     w = _workload(1002, args.scale)
     info = rz.raster_info(w.table, res=w.res, extent=w.extent)
-    for _ in range(args.warmup):
+    # every step is the full workload (seconds of CPU each): the timed steps
+    # stop at REF_BUDGET_S of CPU time, at least three, so that the arm ends
+    # within a few minutes whatever --steps asks for
+    warm = min(args.warmup, 2)
+    for _ in range(warm):
         _oracle_step(w, info, threads=REF_THREADS)
     times, px, edges = [], 0, 0
-    for _ in range(args.steps):
+    while len(times) < args.steps and (len(times) < 3 or sum(times) < REF_BUDGET_S):
         s, px, edges = _oracle_step(w, info, threads=REF_THREADS)
         times.append(s)
     ms = 1e3 * sum(times) / len(times)
     value = px / (ms / 1e3)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "px/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "steps": len(times), "warmup": warm, "steps_requested": args.steps, "warmup_requested": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "scale": args.scale, "polygons": w.table.n_geoms,
                    "vertices": w.table.n_vertices, "raster": [info.nrows, info.ncols]},
