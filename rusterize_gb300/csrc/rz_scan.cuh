@@ -10,49 +10,48 @@ constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr unsigned long long SCAN_TILE = (unsigned long long)SCAN_THREADS * SCAN_ITEMS;
 
+// A block covers SCAN_TILE rows; warp w of the block takes its SCAN_WROWS
+// consecutive rows 32 at a time (lane = row), so every load of a column is
+// one coalesced sweep over 32 neighbouring rows, and a shuffle scan per
+// group of 32 plus a running carry give the warp's prefixes.
+constexpr int SCAN_WARPS = SCAN_THREADS / 32;
+constexpr int SCAN_WROWS = (int)(SCAN_TILE / SCAN_WARPS);
+constexpr int SCAN_GROUPS = SCAN_WROWS / 32;
+
 template <typename T>
-__device__ __forceinline__ T block_exclusive_scan(T v, T* s_warp, T* total) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T incl = v;
+__device__ __forceinline__ T warp_inclusive_scan(T x) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    T t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-    if (lane >= o) incl += t;
+    const T t = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += t;
   }
-  if (lane == 31) s_warp[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    T w = lane < SCAN_THREADS / 32 ? s_warp[lane] : T(0);
-    T wi = w;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      T t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
-      if (lane >= o) wi += t;
-    }
-    if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;
-    if (lane == SCAN_THREADS / 32 - 1) s_warp[32] = wi;
-  }
-  __syncthreads();
-  T res = s_warp[warp] + incl - v;
-  *total = s_warp[32];
-  __syncthreads();
-  return res;
+  return x;
 }
 
 template <typename T, int K>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T* __restrict__ in,
                                                               unsigned long long n, T* __restrict__ sums) {
-  __shared__ T s_warp[33];
-  const unsigned long long base = (unsigned long long)blockIdx.x * SCAN_TILE;
+  __shared__ T s_tot[SCAN_WARPS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned long long r0 = (unsigned long long)blockIdx.x * SCAN_TILE + (unsigned long long)warp * SCAN_WROWS;
   for (int k = 0; k < K; ++k) {
     T acc = 0;
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-      unsigned long long row = base + (unsigned long long)i * SCAN_THREADS + threadIdx.x;
+#pragma unroll 4
+    for (int gi = 0; gi < SCAN_GROUPS; ++gi) {
+      const unsigned long long row = r0 + (unsigned long long)gi * 32 + lane;
       if (row < n) acc += in[row * K + k];
     }
-    T total;
-    block_exclusive_scan<T>(acc, s_warp, &total);
-    if (threadIdx.x == 0) sums[(unsigned long long)blockIdx.x * K + k] = total;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+    if (lane == 0) s_tot[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T total = 0;
+      for (int w = 0; w < SCAN_WARPS; ++w) total += s_tot[w];
+      sums[(unsigned long long)blockIdx.x * K + k] = total;
+    }
+    __syncthreads();
   }
 }
 
@@ -60,29 +59,41 @@ template <typename T, int K>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const T* __restrict__ in, unsigned long long n,
                                                              const T* __restrict__ block_off,
                                                              T* __restrict__ out) {
-  __shared__ T s_warp[33];
-  const unsigned long long base = (unsigned long long)blockIdx.x * SCAN_TILE +
-                                  (unsigned long long)threadIdx.x * SCAN_ITEMS;
+  __shared__ T s_tot[SCAN_WARPS];
+  __shared__ T s_off[SCAN_WARPS + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned long long r0 = (unsigned long long)blockIdx.x * SCAN_TILE + (unsigned long long)warp * SCAN_WROWS;
   for (int k = 0; k < K; ++k) {
-    T vals[SCAN_ITEMS];
-    T sum = 0;
+    T ex[SCAN_GROUPS];  // exclusive prefix of each of this lane's rows within the warp's rows
+    T carry = 0;
 #pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-      unsigned long long row = base + i;
-      vals[i] = row < n ? in[row * K + k] : T(0);
-      sum += vals[i];
+    for (int gi = 0; gi < SCAN_GROUPS; ++gi) {
+      const unsigned long long row = r0 + (unsigned long long)gi * 32 + lane;
+      const T v = row < n ? in[row * K + k] : T(0);
+      const T x = warp_inclusive_scan<T>(v);
+      ex[gi] = carry + x - v;
+      carry += __shfl_sync(0xFFFFFFFFu, x, 31);
     }
-    T total;
-    T run = block_exclusive_scan<T>(sum, s_warp, &total);
-    T off = block_off ? block_off[(unsigned long long)blockIdx.x * K + k] : T(0);
-    run += off;
+    if (lane == 0) s_tot[warp] = carry;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T run = 0;
+      for (int w = 0; w < SCAN_WARPS; ++w) {
+        s_off[w] = run;
+        run += s_tot[w];
+      }
+      s_off[SCAN_WARPS] = run;
+    }
+    __syncthreads();
+    const T boff = block_off ? block_off[(unsigned long long)blockIdx.x * K + k] : T(0);
+    const T off = boff + s_off[warp];
 #pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-      unsigned long long row = base + i;
-      if (row < n) out[row * K + k] = run;
-      run += vals[i];
+    for (int gi = 0; gi < SCAN_GROUPS; ++gi) {
+      const unsigned long long row = r0 + (unsigned long long)gi * 32 + lane;
+      if (row < n) out[row * K + k] = off + ex[gi];
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n * K + k] = off + total;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n * K + k] = boff + s_off[SCAN_WARPS];
+    __syncthreads();  // s_tot / s_off are reused by the next column
   }
 }
 
