@@ -65,8 +65,11 @@ __global__ void k_part_geom(Geo geo, unsigned* part_geom, Ctrl* ctrl) {
 // One warp per part.  Polygon parts get their row range and bitmap window
 // geometry from the min/max of their world coordinates (the world->pixel
 // map is monotone, so transforming the extremes gives the pixel extremes);
-// line and point parts just report their vertex counts.
-__global__ void k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restrict__ jobs, unsigned n_jobs,
+// line and point parts just report their vertex counts.  The kernel waits
+// on dependent loads, so it is held to six blocks per SM (at most 42
+// registers) for more loads in flight.
+__global__ void __launch_bounds__(256, 6) k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restrict__ jobs,
+                                                     unsigned n_jobs,
                             const unsigned* part_geom, PartPlan* plan, unsigned long long* counts /*[P][PC_N]*/,
                             Tune tn, Ctrl* ctrl) {
   if (ctrl->err) return;
