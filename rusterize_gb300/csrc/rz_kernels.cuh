@@ -69,9 +69,8 @@ __global__ void k_part_geom(Geo geo, unsigned* part_geom, Ctrl* ctrl) {
 // on dependent loads, so it is held to six blocks per SM (at most 42
 // registers) for more loads in flight.
 __global__ void __launch_bounds__(256, 6) k_part_prep(Geo geo, Grid g, JobDims one, const JobDims* __restrict__ jobs,
-                                                     unsigned n_jobs,
-                            const unsigned* part_geom, PartPlan* plan, unsigned long long* counts /*[P][PC_N]*/,
-                            Tune tn, Ctrl* ctrl) {
+                                                     unsigned n_jobs, const unsigned* part_geom, PartPlan* plan,
+                                                     unsigned long long* counts /*[P][PC_N]*/, Tune tn, Ctrl* ctrl) {
   if (ctrl->err) return;
   const int lane = threadIdx.x & 31;
   const unsigned long long warp0 = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
