@@ -358,7 +358,7 @@ __device__ __forceinline__ void apply_step(T& c, T v, bool on, T bg, const BgF64
 }
 
 // ---- warp fill -------------------------------------------------------------
-// One warp per bucket.  A warp takes 32 consecutive buckets (one coalesced
+// One warp per bucket.  A warp takes FILL_CHUNK consecutive buckets (one coalesced
 // load of their offsets) and loads the next bucket's records and values
 // while it works on the current one.
 //
@@ -376,7 +376,7 @@ __device__ __forceinline__ void apply_step(T& c, T v, bool on, T bg, const BgF64
 // first / last (buckets of up to OF_WARP_MAX records), and min / max when no
 // written value is the background or NaN, take the order-free pass instead.
 constexpr int FILL_WARPS_PER_BLOCK = 8;
-constexpr int FILL_CHUNK = 32;
+constexpr int FILL_CHUNK = 16;
 
 // Shared memory of one k_fill_warp warp: the sort's records and keys (a
 // power of two of entries, at least sort_max, so that the bitonic network's
@@ -1069,7 +1069,7 @@ __global__ void __launch_bounds__(BIG_WARPS * 32) k_fill_big(FillArgs a) {
 // NaN) equals the pixel's coverage depth: every write after the first adds
 // one and no intermediate count can equal the background.  `any` is 1
 // wherever the depth is non-zero.  Neither needs values or order.  One warp
-// per bucket (32 consecutive buckets per task, the next bucket's records
+// per bucket (FILL_CHUNK consecutive buckets per task, the next bucket's records
 // loaded while the current one is counted); every record is broadcast to the
 // warp and lane l adds its bit l to the counter of the record's word.
 constexpr int DEPTH_WARPS = 8;
