@@ -507,8 +507,10 @@ def _batched_leg(args, ctx, local) -> dict:
 
     st: dict = {}
 
+    wave_bytes = int(args.batch_wave_gb * (1 << 30))
+
     def batch():
-        rasterize_batch_device(jobs, dtype="float32", outs=outs, context=ctx, stats=st)
+        rasterize_batch_device(jobs, dtype="float32", outs=outs, context=ctx, stats=st, wave_bytes=wave_bytes)
 
     def timed(f, reps):
         for _ in range(args.batch_warmup):
@@ -542,7 +544,7 @@ def _batched_leg(args, ctx, local) -> dict:
 
     def batch_ms():
         st1: dict = {}
-        rasterize_batch_device(jobs, dtype="float32", outs=outs, context=ctx, stats=st1)
+        rasterize_batch_device(jobs, dtype="float32", outs=outs, context=ctx, stats=st1, wave_bytes=wave_bytes)
         return st1["ms_device_total"]
 
     legs = set(args.batch_legs.split(","))
@@ -708,6 +710,8 @@ def main():
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="run with the default schedule")
     ap.add_argument("--schedule", default=None,
                     help='fixed schedule of the large-fill leg instead of tuning, e.g. \'{"fill_sort_max": 128}\'')
+    ap.add_argument("--batch-wave-gb", type=float, default=0.0,
+                    help="byte budget of one wave of the batched call (0: the engine's default, 32 GiB)")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--batch-warmup", type=int, default=1)
     ap.add_argument("--batch-legs", default="plain,batched", help="legs of the batched comparison to run")

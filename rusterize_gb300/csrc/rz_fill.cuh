@@ -376,7 +376,7 @@ __device__ __forceinline__ void apply_step(T& c, T v, bool on, T bg, const BgF64
 // first / last (buckets of up to OF_WARP_MAX records), and min / max when no
 // written value is the background or NaN, take the order-free pass instead.
 constexpr int FILL_WARPS_PER_BLOCK = 8;
-constexpr int FILL_CHUNK = 16;
+constexpr int FILL_CHUNK = 4;
 
 // Shared memory of one k_fill_warp warp: the sort's records and keys (a
 // power of two of entries, at least sort_max, so that the bitonic network's
