@@ -161,8 +161,11 @@ def rasterize_sparse(table, nrows, ncols, xmin, xmax, ymin, ymax, xres, yres, *,
     try:
         rows = np.ctypeslib.as_array(ctypes.cast(rows_p, ctypes.POINTER(ctypes.c_uint64)), (max(n, 1),))[:n].copy()
         cols = np.ctypeslib.as_array(ctypes.cast(cols_p, ctypes.POINTER(ctypes.c_uint64)), (max(n, 1),))[:n].copy()
-        raw = ctypes.string_at(vals_p, n * dt.itemsize) if n else b""
-        out_vals = np.frombuffer(raw, dtype=dt).copy()
+        if n:
+            raw = np.ctypeslib.as_array(ctypes.cast(vals_p, ctypes.POINTER(ctypes.c_uint8)), shape=(n * dt.itemsize,))
+            out_vals = raw.view(dt).copy()
+        else:
+            out_vals = np.empty(0, dtype=dt)
     finally:
         for p_ in (rows_p, cols_p, vals_p):
             lib.rzo_free(p_)

@@ -137,6 +137,16 @@ def rasterize_table(table: GeometryTable, info: RasterInfo, *, values=None, fn: 
     return out
 
 
+def copy_from_address(ptr: int, count: int, dtype) -> np.ndarray:
+    """A numpy copy of `count` elements of `dtype` at host address `ptr`
+    (any size: a view of the memory, then one copy)."""
+    dt = np.dtype(dtype)
+    if count == 0:
+        return np.empty(0, dtype=dt)
+    raw = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_uint8)), shape=(count * dt.itemsize,))
+    return raw.view(dt).copy()
+
+
 def rasterize_table_sparse(table: GeometryTable, info: RasterInfo, *, values=None, fn: str = "last",
                            dtype: str = "float64", bands: np.ndarray | None = None, n_bands: int | None = None,
                            all_touched: bool = False, context: _lib.Context | None = None,
@@ -185,9 +195,7 @@ def rasterize_table_sparse(table: GeometryTable, info: RasterInfo, *, values=Non
         n = int(v.count)
 
         def arr(ptr, count, dt):
-            if count == 0:
-                return np.empty(0, dtype=dt)
-            return np.frombuffer(ctypes.string_at(ptr, count * np.dtype(dt).itemsize), dtype=dt).copy()
+            return copy_from_address(ptr, count, dt)
 
         band_counts = arr(v.band_counts, int(v.n_bands), np.uint64)
         rows = arr(v.rows, n, np.uint64)

@@ -71,3 +71,13 @@ def test_batch_job_structs():
     with pytest.raises(ValueError, match="pixel function"):
         _job_struct(BatchJob(t, _info(8, 8), fn="mean"), np.dtype("float64"), keep, device=False)
     assert ctypes.sizeof(_lib.RzJob) == 80 + 8 + 8 + 72 + 4 + 4 + 8
+
+
+def test_copy_from_address_any_dtype_and_empty():
+    from rusterize_gb300.engine import copy_from_address
+
+    for dt in ("uint8", "int16", "float32", "uint64", "float64"):
+        a = (np.arange(1000) * 3 - 7).astype(dt)
+        b = copy_from_address(a.ctypes.data, len(a), dt)
+        assert b.dtype == np.dtype(dt) and np.array_equal(a, b) and b.ctypes.data != a.ctypes.data
+    assert copy_from_address(0, 0, "float64").shape == (0,)
