@@ -1162,6 +1162,8 @@ static rz_status replay_impl(rz_context* ctx, const uint64_t* band_counts, uint3
   unsigned long long bg_bits = 0;
   std::memcpy(&bg_bits, background, tsize);
   int launches = 0;
+  PageToucher toucher;  // a host output's pages, faulted in while the device replays
+  if (!out_dev) toucher.start(out, (size_t)(px * tsize));
 
   if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[0], s));
   RZ_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), s));
@@ -1216,6 +1218,7 @@ static rz_status replay_impl(rz_context* ctx, const uint64_t* band_counts, uint3
   RZ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
   RZ_CUDA(cudaStreamSynchronize(s));
   if (ctx->h_ctrl->err) return ctrl_error(*ctx->h_ctrl, err, errlen);
+  toucher.join();
   if (!out_dev) RZ_CUDA(cudaMemcpyAsync(out, d_ras, px * tsize, cudaMemcpyDeviceToHost, s));
   if (timing) RZ_CUDA(cudaEventRecord(ctx->ev[6], s));
   RZ_CUDA(cudaStreamSynchronize(s));
