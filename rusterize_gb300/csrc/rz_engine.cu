@@ -305,10 +305,28 @@ int launch_coverage(const Geo& geo, const Grid& gr, const PartTables& t, const R
 // band fills.
 constexpr int kFillBands = 8;
 
+// A host array that is not zero-filled: a sparse result's columns are
+// written whole by the copies from the device.
+struct HostArray {
+  unsigned char* p = nullptr;
+  size_t bytes = 0;
+  HostArray() = default;
+  HostArray(const HostArray&) = delete;
+  HostArray& operator=(const HostArray&) = delete;
+  ~HostArray() { std::free(p); }
+  bool alloc(size_t n) {
+    std::free(p);
+    p = static_cast<unsigned char*>(std::malloc(n ? n : 1));
+    bytes = p ? n : 0;
+    return p != nullptr;
+  }
+};
+
 // Host copy of a sparse (COO) result.
 struct rz_sparse {
-  std::vector<uint64_t> band_counts, rows, cols;
-  std::vector<unsigned char> values;
+  std::vector<uint64_t> band_counts;
+  HostArray rows, cols, values;
+  uint64_t count = 0;
   uint32_t n_bands = 1;
   rz_dtype dtype = RZ_F64;
 };
@@ -927,9 +945,14 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
         launches += 2 + scan<unsigned long long, 1>(cnt, off, n, static_cast<unsigned long long*>(sat(o_st64)), s);
         RZ_CUDA(cudaMemcpyAsync(&total, off + n, 8, cudaMemcpyDeviceToHost, s));
         RZ_CUDA(cudaStreamSynchronize(s));
-        sp->rows.resize(total);
-        sp->cols.resize(total);
-        sp->values.resize(total * tsize);
+        sp->count = total;
+        if (!sp->rows.alloc(8 * total) || !sp->cols.alloc(8 * total) || !sp->values.alloc(tsize * total))
+          return fail(err, errlen, RZ_OUT_OF_MEMORY, "cannot allocate %llu sparse triplets on the host", total);
+        // their pages are faulted in by host threads while the device emits
+        PageToucher touch_rows, touch_cols, touch_vals;
+        touch_rows.start(sp->rows.p, 8 * total);
+        touch_cols.start(sp->cols.p, 8 * total);
+        touch_vals.start(sp->values.p, tsize * total);
         if (total) {
           // the triplet arrays go after the sort scratch (grow-only buffer)
           const size_t o_rows = (base_bytes + 255) & ~size_t(255);
@@ -967,9 +990,12 @@ static rz_status burn_impl(rz_context* ctx, const rz_geoms* g, const void* value
           }
           ++launches;
           RZ_CUDA(cudaGetLastError());
-          RZ_CUDA(cudaMemcpyAsync(sp->rows.data(), trows, 8 * total, cudaMemcpyDeviceToHost, s));
-          RZ_CUDA(cudaMemcpyAsync(sp->cols.data(), tcols, 8 * total, cudaMemcpyDeviceToHost, s));
-          RZ_CUDA(cudaMemcpyAsync(sp->values.data(), tvals, tsize * total, cudaMemcpyDeviceToHost, s));
+          touch_rows.join();
+          touch_cols.join();
+          touch_vals.join();
+          RZ_CUDA(cudaMemcpyAsync(sp->rows.p, trows, 8 * total, cudaMemcpyDeviceToHost, s));
+          RZ_CUDA(cudaMemcpyAsync(sp->cols.p, tcols, 8 * total, cudaMemcpyDeviceToHost, s));
+          RZ_CUDA(cudaMemcpyAsync(sp->values.p, tvals, tsize * total, cudaMemcpyDeviceToHost, s));
         }
       }
       RZ_CUDA(cudaMemcpyAsync(sp->band_counts.data(), bcnt, 8 * nb, cudaMemcpyDeviceToHost, s));
@@ -1045,13 +1071,13 @@ extern "C" rz_status rz_rasterize_sparse(rz_context* ctx, const rz_geoms* g, con
 
 extern "C" rz_status rz_sparse_view_get(const rz_sparse* sp, rz_sparse_view* out) {
   if (!sp || !out) return RZ_INVALID_ARGUMENT;
-  out->count = sp->rows.size();
+  out->count = sp->count;
   out->n_bands = sp->n_bands;
   out->dtype = sp->dtype;
   out->band_counts = sp->band_counts.data();
-  out->rows = sp->rows.data();
-  out->cols = sp->cols.data();
-  out->values = sp->values.data();
+  out->rows = reinterpret_cast<const uint64_t*>(sp->rows.p);
+  out->cols = reinterpret_cast<const uint64_t*>(sp->cols.p);
+  out->values = sp->values.p;
   return RZ_OK;
 }
 

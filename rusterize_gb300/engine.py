@@ -137,6 +137,35 @@ def rasterize_table(table: GeometryTable, info: RasterInfo, *, values=None, fn: 
     return out
 
 
+class _SparseResult:
+    """Owner of an engine sparse result (rz_sparse): numpy views of its
+    columns keep it alive, and it is freed with the last of them."""
+
+    def __init__(self, lib, handle):
+        self._lib = lib
+        self._h = handle
+
+    def view(self, ptr: int, count: int, dtype) -> np.ndarray:
+        dt = np.dtype(dtype)
+        if count == 0 or not ptr:
+            return np.empty(0, dtype=dt)
+        nbytes = count * dt.itemsize
+        # a subclass of the ctypes array type can carry the owner; numpy's
+        # buffer keeps the ctypes object, and so the owner, alive
+        buf_t = type("_SparseColumn", (ctypes.c_uint8 * nbytes,), {})
+        buf = buf_t.from_address(ptr)
+        buf._owner = self
+        return np.frombuffer(buf, dtype=dt, count=count)
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._lib.rz_sparse_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
 def copy_from_address(ptr: int, count: int, dtype) -> np.ndarray:
     """A numpy copy of `count` elements of `dtype` at host address `ptr`
     (any size: a view of the memory, then one copy)."""
@@ -189,20 +218,16 @@ def rasterize_table_sparse(table: GeometryTable, info: RasterInfo, *, values=Non
                                      _lib.PIXEL_FNS[fn], _lib.DTYPES[dtype], flags, ctypes.byref(h),
                                      ctypes.byref(st_c), e, len(e))
     _lib.raise_for(st, e.value)
-    try:
-        v = _lib.RzSparseView()
-        lib.rz_sparse_view_get(h, ctypes.byref(v))
-        n = int(v.count)
-
-        def arr(ptr, count, dt):
-            return copy_from_address(ptr, count, dt)
-
-        band_counts = arr(v.band_counts, int(v.n_bands), np.uint64)
-        rows = arr(v.rows, n, np.uint64)
-        cols = arr(v.cols, n, np.uint64)
-        vals = arr(v.values, n, np_dt)
-    finally:
-        lib.rz_sparse_free(h)
+    owner = _SparseResult(lib, h)
+    v = _lib.RzSparseView()
+    lib.rz_sparse_view_get(h, ctypes.byref(v))
+    n = int(v.count)
+    band_counts = copy_from_address(v.band_counts, int(v.n_bands), np.uint64)
+    # the triplet columns are views of the engine's arrays (no copy of the
+    # stream); the result is freed when the last of them is collected
+    rows = owner.view(v.rows, n, np.uint64)
+    cols = owner.view(v.cols, n, np.uint64)
+    vals = owner.view(v.values, n, np_dt)
     if stats is not None:
         stats.update(st_c.as_dict())
     return band_counts, rows, cols, vals
