@@ -62,9 +62,11 @@ struct Tune {
   int fill_sort_max;     // the warp fill sorts up to this many records of a tile (FILL_WARP_MAX..FILL_WARP_SORT)
 };
 
-// Fill: buckets with at most FILL_WARP_SORT records are sorted and applied by
-// one warp; larger ones go to the per-word path, which takes at most
-// BIG_CAP records of one word at a time.
+// Fill: buckets with at most the schedule's sort threshold (<= FILL_WARP_SORT)
+// records are sorted and applied by one warp; larger ones go to the per-word
+// path, which takes at most BIG_CAP records of one word at a time.  The
+// order-free functions (first, last, and min / max without background or NaN
+// values) skip the sort.
 constexpr int FILL_WARP_MAX = 64;    // records held in registers (two per lane)
 constexpr int FILL_WARP_SORT = 256;  // records sorted in shared memory by one warp
 constexpr int BIG_CAP = 1024;
