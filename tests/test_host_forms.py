@@ -81,3 +81,30 @@ def test_copy_from_address_any_dtype_and_empty():
         b = copy_from_address(a.ctypes.data, len(a), dt)
         assert b.dtype == np.dtype(dt) and np.array_equal(a, b) and b.ctypes.data != a.ctypes.data
     assert copy_from_address(0, 0, "float64").shape == (0,)
+
+
+def test_sparse_result_views_free_the_engine_result_with_the_last_view():
+    import gc
+
+    from rusterize_gb300.engine import _SparseResult
+
+    freed = []
+
+    class _FakeLib:
+        def rz_sparse_free(self, h):
+            freed.append(h)
+
+    backing = (ctypes.c_uint64 * 10)(*range(10))
+    owner = _SparseResult(_FakeLib(), 1234)
+    a = owner.view(ctypes.addressof(backing), 10, np.uint64)
+    b = owner.view(ctypes.addressof(backing), 5, np.float64)
+    assert owner.view(0, 0, np.uint8).shape == (0,)
+    del owner
+    gc.collect()
+    assert freed == [] and a.tolist() == list(range(10)) and len(b) == 5
+    del a
+    gc.collect()
+    assert freed == []
+    del b
+    gc.collect()
+    assert freed == [1234]
